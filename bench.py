@@ -1,0 +1,369 @@
+#!/usr/bin/env python3
+"""Benchmark: single-source BFS on RMAT scale 22 (edge factor 16, a/b/c/d =
+.57/.19/.19/.05, symmetrised, deduplicated, no self-loops, seeded), 64 seeded
+non-isolated sources run one at a time.
+
+One step = 64 BFS launches, one per source, with the graph resident in HBM.
+  value  GTEPS = sum over the step's BFS of E_R (out-degrees of reached
+         vertices) / device time of the step (CUDA events on the graph's
+         stream, synchronize on both sides), levels written to device buffers.
+  e2e    the same metric through the public C ABI call dfq_bfs() with HOST
+         (pinned) level buffers: launch + device->host copy of every level
+         array inside the timed region.
+  roofline  algorithmic bytes per BFS = 4*E_R + 8*|R| + 4*N over the average
+         launch time of the BFS kernel (events around each launch), against
+         the measured HBM copy bandwidth.
+  cpu_baseline  the oracle (the reference's serial CPU BFS, restated in C) on
+         a bounded sample of the sources, 1 host core.
+  reference_gpu the reference's own kernel (design/shared-q/atomic-sa/our-sep/
+         upper-bound/bfs.cu) compiled from its sources, same graph and
+         sources, its "- Time" definition.
+
+--impl reference: the reference's CPU path (the oracle port; the reference's
+serial BFS is inlined in its main() and cannot be built alone) on the same
+workload, one source per step.
+Multi-GPU (torchrun): replicas only - each rank runs the full step on its own
+copy of the graph (weak scaling); value sums all ranks' edges over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path[:0] = [str(ROOT / "dfq-bfs_gb300"), str(ROOT)]
+
+import numpy as np  # noqa: E402
+
+METRIC = "BFS GTEPS (RMAT-22 EF16, 64 sources one at a time)"
+UNIT = "GTEPS"
+WORKLOAD = {"workload": "rmat22_ef16_64src", "graph": "RMAT scale 22, edge factor 16, a=.57 b=.19 c=.19 d=.05",
+            "symmetrized": True, "dedup": True, "self_loops": False, "seed": 1, "sources": 64,
+            "source_seed": 1, "l2": "inputs larger than L2 (column array ~0.5 GB > 129 MB L2)"}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        j = json.loads(p.read_text())
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_graph():
+    import dfqbfs as d
+    cache = Path(os.environ.get("DFQ_BENCH_CACHE", "/tmp")) / "dfq_rmat22_ef16_s1.bin"
+    if cache.exists():
+        try:
+            return d.load(cache, "bin")
+        except d.DfqError:
+            pass
+    g = d.gen_rmat(22, 16, 0.57, 0.19, 0.19, seed=1)
+    try:
+        g.save(cache, "bin")
+    except d.DfqError:
+        pass
+    return g
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+                out, _ = self.p.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return ws, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allreduce_max(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_sample(g, sources, budget_s=15.0):
+    """Oracle BFS (1 core) over sources until ~budget_s of CPU work."""
+    import oracle
+    edges, t_total, done = 0, 0.0, 0
+    for s in sources:
+        t0 = time.perf_counter()
+        lv = oracle.bfs(g.offsets, g.cols, int(s))
+        t_total += time.perf_counter() - t0
+        edges += oracle.reached_edges(g.offsets, lv)
+        done += 1
+        if t_total >= budget_s:
+            break
+    return edges, t_total, done
+
+
+def run_reference(args, ws, rank, pg):
+    """The reference's CPU path (oracle port), one source per step."""
+    if rank != 0:
+        return 0
+    import oracle
+    g = load_graph()
+    srcs = g.pick_sources(64, seed=1)
+    oracle.lib()
+    for i in range(args.warmup):
+        oracle.bfs(g.offsets, g.cols, int(srcs[i % 64]))
+    edges, ts = 0, []
+    for i in range(args.steps):
+        s = int(srcs[i % 64])
+        t0 = time.perf_counter()
+        lv = oracle.bfs(g.offsets, g.cols, s)
+        ts.append(time.perf_counter() - t0)
+        edges += oracle.reached_edges(g.offsets, lv)
+    tot = sum(ts)
+    val = edges / tot / 1e9
+    line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
+            "config": dict(WORKLOAD, step="one source (serial CPU BFS)"), "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"{args.steps} sources of the 64, one serial BFS each"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="dfq", choices=["dfq", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference GPU kernel")
+    ap.add_argument("--sources", type=int, default=64)
+    args = ap.parse_args()
+    ws, rank, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        r = run_reference(args, ws, rank, pg)
+        return r
+    args.warmup = max(args.warmup, 3)
+
+    import torch
+    import dfqbfs as d
+    torch.cuda.set_device(local)
+    t_gen = time.perf_counter()
+    g = load_graph()
+    t_gen = time.perf_counter() - t_gen
+    srcs = g.pick_sources(64, seed=1)[: args.sources]
+    dg = d.Graph(g)
+    n = g.n
+    stream = torch.cuda.ExternalStream(dg.stream)
+    levels = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)]
+
+    # per-source E_R and |R| from one untimed pass (checked against the kernel's own counters)
+    er, rr = [], []
+    for s in srcs:
+        dg.launch(int(s), levels[0])
+        st = dg.last_stats()
+        er.append(st.edges)
+        rr.append(st.reached)
+    er, rr = np.array(er, np.int64), np.array(rr, np.int64)
+    step_edges = int(er.sum())
+    step_bytes = int((4 * er + 8 * rr + 4 * n).sum())
+
+    def step(evs=None):
+        for i, s in enumerate(srcs):
+            if evs is not None:
+                evs[i][0].record(stream)
+            dg.launch(int(s), levels[i & 1])
+            if evs is not None:
+                evs[i][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    dg.sync()
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in srcs]
+           for _ in range(args.steps)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(pg)
+    torch.cuda.synchronize()
+    with Clocks(local) as ck:
+        t0.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    dg.sync()
+    barrier(pg)
+    ms_total = t0.elapsed_time(t1)
+    launch_ms = [a.elapsed_time(b) for row in evs for (a, b) in row]
+    ms_max = allreduce_max(pg, ms_total)
+    total_edges = allreduce_sum(pg, float(step_edges * args.steps))
+    value = total_edges / (ms_max * 1e-3) / 1e9
+    hbm, peak_kind = peaks()
+    avg_launch_ms = float(np.mean(launch_ms))
+    bytes_per_launch = step_bytes / len(srcs)
+    achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9
+
+    # e2e: public API with pinned host level buffers (launch + D2H inside the timed region)
+    host_lv = [torch.empty(n, dtype=torch.int32, pin_memory=True) for _ in range(2)]
+    for i, s in enumerate(srcs[:4]):
+        dg.bfs(int(s), levels_out=host_lv[i & 1])
+    e2e_steps = max(1, min(args.steps, 3))
+    barrier(pg)
+    te0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for i, s in enumerate(srcs):
+            dg.bfs(int(s), levels_out=host_lv[i & 1])
+    te = time.perf_counter() - te0
+    te = allreduce_max(pg, te)
+    e2e_edges = allreduce_sum(pg, float(step_edges * e2e_steps))
+    e2e = e2e_edges / te / 1e9
+    # parity spot check of the e2e output against the device run
+    ok_parity = bool(torch.equal(host_lv[(len(srcs) - 1) & 1], levels[(len(srcs) - 1) & 1].cpu()))
+
+    traffic = None
+    tp = ROOT / "profiles" / "traffic_rmat22.txt"
+    if tp.exists():
+        for line in tp.read_text().splitlines():
+            if line.startswith("dram_bytes_per_launch="):
+                traffic = float(line.split("=", 1)[1])
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
+           "config": dict(WORKLOAD, n=n, e=g.e, parallelism=f"replicas x{ws}", opts=dg.opts().as_dict(),
+                          edges_per_step=step_edges, gen_s=round(t_gen, 2)),
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                        "kernel": "dfq_bfs_kernel", "bytes_alg_per_launch": bytes_per_launch,
+                        "avg_launch_ms": avg_launch_ms},
+           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * len(srcs),
+                   "d2h_bytes_per_step": 4 * n * len(srcs), "api": "dfq_bfs (host levels)",
+                   "steps": e2e_steps, "parity_vs_device": ok_parity},
+           "gpu_launches": args.steps * len(srcs),
+           "clocks": ck.summary(),
+           "per_bfs_ms_median": float(np.median(launch_ms)),
+           "gteps_median_source": float(np.median(er / (np.array(launch_ms[:len(srcs)]) * 1e-3) / 1e9))}
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        oracle.lib()
+        edges, tcpu, nsrc = cpu_sample(g, srcs, budget_s=15.0)
+        out["cpu_baseline"] = {"value": edges / tcpu / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"{nsrc} of the 64 sources, serial oracle BFS, {tcpu:.1f} s"}
+    if rank == 0 and not args.no_ref_gpu:
+        out["reference_gpu"] = reference_gpu(g, srcs)
+    dg.close()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+def reference_gpu(g, srcs, max_sources=16):
+    """The reference kernel on the same graph: median GTEPS over sources."""
+    try:
+        import oracle
+        from oracle import refgpu
+    except Exception as e:  # pragma: no cover
+        return {"unavailable": f"import failed: {e}"}
+    if not refgpu.available("dfq"):
+        return {"unavailable": "reference cubin not built (reference sources absent where build() ran)"}
+    res = {"kernel": "design/shared-q/atomic-sa/our-sep/upper-bound/bfs.cu", "sources": 0}
+    try:
+        with refgpu.RefGpu("dfq") as ref:
+            ref.load(g.offsets, g.cols)
+            gteps, ms, errors = [], [], 0
+            for s in srcs[:max_sources]:
+                want = oracle.bfs(g.offsets, g.cols, int(s))
+                ok, why = ref.safe_for(want)
+                if not ok:
+                    return {"unavailable": f"refused (queue bounds): {why}"}
+                ref.bfs(int(s))  # warm
+                lv, t = ref.bfs(int(s))
+                errors += oracle.compare(want, lv)["near_errors"]
+                ms.append(t)
+                gteps.append(oracle.reached_edges(g.offsets, want) / (t * 1e-3) / 1e9)
+            res.update({"sources": len(ms), "ms_median": float(np.median(ms)),
+                        "gteps_median": float(np.median(gteps)),
+                        "gteps_aggregate": float(sum(g_ * m for g_, m in zip(gteps, ms)) / sum(ms)),
+                        "errors": int(errors), "grid": ref.grid})
+    except Exception as e:
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+    return res
+
+
+if __name__ == "__main__":
+    sys.exit(main())

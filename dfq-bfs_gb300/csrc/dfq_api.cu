@@ -1,0 +1,464 @@
+// Host side of the libdfq C ABI: device-resident graphs, per-graph workspace,
+// cooperative launch of the persistent DFQ kernel, statistics and errors.
+//
+// Replaces the reference host path of
+// design/shared-q/atomic-sa/our-sep/upper-bound/bfs.cu:
+//   :194-199,273-277  managed allocation + prefetch   -> dfq_graph_create
+//   :255-268,283      occupancy-sized cooperative launch -> launch_bfs
+//   :279-288          events around launch + sync      -> dfq_bfs (kernel_ms)
+//   :290-300          Dist / Touch / Error             -> dfq_stats
+#include "common.hpp"
+#include "dfq_kernel.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+using namespace dfq;
+
+#define CUDA_TRY(call)                                                                           \
+    do {                                                                                         \
+        cudaError_t err_ = (call);                                                               \
+        if (err_ != cudaSuccess)                                                                 \
+            return fail(DFQ_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(err_),    \
+                        __FILE__, __LINE__);                                                     \
+    } while (0)
+
+struct dfq_graph {
+    int device = 0;
+    int sms = 0;
+    int32_t n = 0;
+    int64_t e = 0;
+    dfq_opts opts{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int32_t* offsets = nullptr;
+    int32_t* cols = nullptr;
+    // workspace
+    int32_t* levels_tmp = nullptr;
+    int32_t* parents_tmp = nullptr;
+    unsigned* bitmap = nullptr;
+    int bitmap_words = 0;
+    int2* ovf[2] = {nullptr, nullptr};
+    int32_t* ovfv[2] = {nullptr, nullptr};
+    int4* large[2] = {nullptr, nullptr};
+    int32_t* piece_owner[2] = {nullptr, nullptr};
+    int large_cap = 0;
+    int piece_cap = 0;
+    dfqk::Control* ctl = nullptr;
+    dfqk::Control* ctl_host = nullptr;  // pinned copy for status / stats
+    bool persist_set = false;
+};
+
+namespace {
+
+constexpr int kMinLargeDegree = 32;
+constexpr int kMinPiece = 64;
+constexpr int kColsPad = 32;
+
+using KernelFn = void (*)(dfqk::Params);
+
+KernelFn pick_kernel(int B, bool par) {
+    switch (B) {
+        case 256: return par ? dfqk::dfq_bfs_kernel<256, true> : dfqk::dfq_bfs_kernel<256, false>;
+        case 512: return par ? dfqk::dfq_bfs_kernel<512, true> : dfqk::dfq_bfs_kernel<512, false>;
+        case 1024: return par ? dfqk::dfq_bfs_kernel<1024, true> : dfqk::dfq_bfs_kernel<1024, false>;
+        default: return nullptr;
+    }
+}
+
+int validate_opts(const dfq_opts& o) {
+    if (o.block_threads != 256 && o.block_threads != 512 && o.block_threads != 1024)
+        return fail(DFQ_EINVAL, "block_threads must be 256, 512 or 1024 (got %d)", o.block_threads);
+    if (o.blocks_per_sm < 0 || o.blocks_per_sm > 8) return fail(DFQ_EINVAL, "blocks_per_sm must be in [0,8]");
+    if (o.large_min_degree < kMinLargeDegree)
+        return fail(DFQ_EINVAL, "large_min_degree must be >= %d", kMinLargeDegree);
+    if (o.medium_min_degree < 1) return fail(DFQ_EINVAL, "medium_min_degree must be >= 1");
+    if (o.piece_edges < kMinPiece || o.piece_edges % 64 || o.piece_edges > 16384)
+        return fail(DFQ_EINVAL, "piece_edges must be a multiple of 64 in [64,16384]");
+    if (o.local_queue_cap < 0 || o.local_queue_cap > 8192)
+        return fail(DFQ_EINVAL, "local_queue_cap must be in [0,8192]");
+    if (o.timeout_ms < 1) return fail(DFQ_EINVAL, "timeout_ms must be >= 1");
+    const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges);
+    if (L.bytes > 200 * 1024)
+        return fail(DFQ_EINVAL, "options need %d bytes of shared memory per block (max 204800)", L.bytes);
+    return DFQ_OK;
+}
+
+template <class T>
+int dev_alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t err = cudaMalloc((void**)p, sizeof(T) * count);
+    if (err != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(err == cudaErrorMemoryAllocation ? DFQ_ENOMEM : DFQ_ECUDA,
+                    "cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(err));
+    }
+    return DFQ_OK;
+}
+
+bool is_device_ptr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+__global__ void validate_csr_kernel(const int32_t* off, const int32_t* cols, int32_t n, int64_t e,
+                                    int* bad) {
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = tid; i < n; i += nth)
+        if (off[i + 1] < off[i]) atomicCAS(bad, 0, 1);
+    if (tid == 0 && (off[0] != 0 || (int64_t)off[n] != e)) atomicCAS(bad, 0, 2);
+    for (int64_t k = tid; k < e; k += nth)
+        if ((uint32_t)cols[k] >= (uint32_t)n) atomicCAS(bad, 0, 3);
+}
+
+int map_device_status(const dfqk::Control& c) {
+    switch (c.status) {
+        case dfqk::kErrNone: return DFQ_OK;
+        case dfqk::kErrBarrierTimeout:
+            return fail(DFQ_ETIMEOUT, "grid barrier wait timed out (block %d, target %u)", c.err_info[0],
+                        (unsigned)c.err_info[1]);
+        case dfqk::kErrTmaTimeout:
+            return fail(DFQ_ETIMEOUT, "bulk-copy wait timed out (block %d, edge %d)", c.err_info[0],
+                        c.err_info[1]);
+        case dfqk::kErrQueueCap:
+            return fail(DFQ_EDEVICE, "queue capacity exceeded (index %d, capacity %d)", c.err_info[0],
+                        c.err_info[1]);
+        default: return fail(DFQ_EDEVICE, "device reported status %d", c.status);
+    }
+}
+
+void release(dfq_graph* g) {
+    if (!g) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    cudaFree(g->offsets);
+    cudaFree(g->cols);
+    cudaFree(g->levels_tmp);
+    cudaFree(g->parents_tmp);
+    cudaFree(g->bitmap);
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(g->ovf[i]);
+        cudaFree(g->ovfv[i]);
+        cudaFree(g->large[i]);
+        cudaFree(g->piece_owner[i]);
+    }
+    cudaFree(g->ctl);
+    if (g->ctl_host) cudaFreeHost(g->ctl_host);
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    cudaSetDevice(prev);
+    delete g;
+}
+
+int apply_persist(dfq_graph* g) {
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, g->device));
+    cudaStreamAttrValue attr;
+    memset(&attr, 0, sizeof attr);
+    if (g->opts.l2_persist && prop.persistingL2CacheMaxSize > 0 && prop.accessPolicyMaxWindowSize > 0) {
+        size_t bytes = sizeof(unsigned) * (size_t)g->bitmap_words;
+        bytes = std::min(bytes, (size_t)prop.accessPolicyMaxWindowSize);
+        size_t limit = std::min(bytes, (size_t)prop.persistingL2CacheMaxSize);
+        CUDA_TRY(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, limit));
+        attr.accessPolicyWindow.base_ptr = g->bitmap;
+        attr.accessPolicyWindow.num_bytes = bytes;
+        attr.accessPolicyWindow.hitRatio = 1.0f;
+        attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        CUDA_TRY(cudaStreamSetAttribute(g->stream, cudaStreamAttributeAccessPolicyWindow, &attr));
+        g->persist_set = true;
+    } else if (g->persist_set) {
+        attr.accessPolicyWindow.num_bytes = 0;
+        CUDA_TRY(cudaStreamSetAttribute(g->stream, cudaStreamAttributeAccessPolicyWindow, &attr));
+        g->persist_set = false;
+    }
+    return DFQ_OK;
+}
+
+// Queue control-block reset + the cooperative kernel on g->stream.
+int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
+    const dfq_opts& o = g->opts;
+    const bool par = parents != nullptr;
+    KernelFn k = pick_kernel(o.block_threads, par);
+    if (!k) return fail(DFQ_EINVAL, "no kernel for block_threads=%d", o.block_threads);
+    const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges);
+    CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.bytes));
+    int per_sm = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k, o.block_threads, lay.bytes));
+    if (per_sm < 1) return fail(DFQ_EINVAL, "kernel does not fit on an SM with these options");
+    if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
+    const int grid = g->sms * per_sm;
+
+    dfqk::Params p;
+    memset(&p, 0, sizeof p);
+    p.offsets = g->offsets;
+    p.cols = g->cols;
+    p.n = g->n;
+    p.src = src;
+    p.levels = levels;
+    p.parents = parents;
+    p.bitmap = g->bitmap;
+    p.bitmap_words = g->bitmap_words;
+    for (int i = 0; i < 2; ++i) {
+        p.ovf[i] = g->ovf[i];
+        p.ovfv[i] = g->ovfv[i];
+        p.large[i] = g->large[i];
+        p.piece_owner[i] = g->piece_owner[i];
+    }
+    p.large_cap = g->large_cap;
+    p.piece_cap = g->piece_cap;
+    p.ctl = g->ctl;
+    p.medium_min = o.medium_min_degree;
+    p.large_min = o.large_min_degree;
+    p.piece_edges = o.piece_edges;
+    p.local_cap = o.local_queue_cap;
+    p.probe_first = o.probe_first;
+    p.use_tma = o.use_tma;
+    p.timeout_ns = (long long)o.timeout_ms * 1000000LL;
+
+    CUDA_TRY(cudaMemsetAsync(g->ctl, 0, sizeof(dfqk::Control), g->stream));
+    void* args[] = {&p};
+    CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(o.block_threads), args, lay.bytes,
+                                         g->stream));
+    return DFQ_OK;
+}
+
+int fill_stats(dfq_graph* g, dfq_stats* st) {
+    CUDA_TRY(cudaMemcpyAsync(g->ctl_host, g->ctl, sizeof(dfqk::Control), cudaMemcpyDeviceToHost, g->stream));
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    const dfqk::Control& c = *g->ctl_host;
+    if (st) {
+        st->depth = c.stats.depth;
+        st->levels = c.stats.levels;
+        st->reached = (int64_t)c.stats.claims + 1;
+        st->edges = (int64_t)c.stats.edges;
+        st->overflow = (int64_t)c.stats.overflow;
+        st->large = (int64_t)c.stats.large;
+    }
+    return map_device_status(c);
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+void dfq_opts_default(dfq_opts* o) {
+    if (!o) return;
+    o->block_threads = 512;
+    o->blocks_per_sm = 0;
+    o->medium_min_degree = 32;
+    o->large_min_degree = 1024;
+    o->local_queue_cap = 1024;
+    o->piece_edges = 2048;
+    o->probe_first = 1;
+    o->l2_persist = 0;
+    o->use_tma = 1;
+    o->timeout_ms = 5000;
+}
+
+int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int64_t e, const dfq_opts* opts,
+                     dfq_graph** out) {
+    clear_error();
+    if (!out) return fail(DFQ_EINVAL, "dfq_graph_create: out is null");
+    *out = nullptr;
+    if (!offsets || (e > 0 && !cols) || n < 1 || e < 0 || e >= ((int64_t)1 << 31))
+        return fail(DFQ_EINVAL, "dfq_graph_create: need offsets, cols, 1 <= n, 0 <= e < 2^31");
+    dfq_opts o;
+    dfq_opts_default(&o);
+    if (opts) o = *opts;
+    if (o.block_threads == 0) o.block_threads = 512;
+    if (o.local_queue_cap == 0) o.local_queue_cap = 1024;
+    if (o.timeout_ms == 0) o.timeout_ms = 5000;
+    int rc = validate_opts(o);
+    if (rc) return rc;
+
+    const bool dev_in = is_device_ptr(offsets);
+    if (!dev_in) {  // host input: validate here (the reference validates nothing)
+        if (offsets[0] != 0 || (int64_t)offsets[n] != e)
+            return fail(DFQ_EFORMAT, "offsets[0] must be 0 and offsets[n] must equal e");
+        for (int32_t u = 0; u < n; ++u)
+            if (offsets[u + 1] < offsets[u]) return fail(DFQ_EFORMAT, "offsets decrease at vertex %d", u);
+        for (int64_t k = 0; k < e; ++k)
+            if ((uint32_t)cols[k] >= (uint32_t)n)
+                return fail(DFQ_EFORMAT, "cols[%lld] = %d outside [0,%d)", (long long)k, cols[k], n);
+    }
+
+    dfq_graph* g = new dfq_graph();
+    g->n = n;
+    g->e = e;
+    g->opts = o;
+    cudaGetDevice(&g->device);
+    cudaDeviceProp prop;
+    cudaError_t err = cudaGetDeviceProperties(&prop, g->device);
+    if (err != cudaSuccess) { release(g); return fail(DFQ_ECUDA, "no CUDA device: %s", cudaGetErrorString(err)); }
+    if (!prop.cooperativeLaunch) { release(g); return fail(DFQ_ECUDA, "device does not support cooperative launch"); }
+    g->sms = prop.multiProcessorCount;
+#define G_TRY(x) do { int rc_ = (x); if (rc_) { release(g); return rc_; } } while (0)
+#define G_CUDA(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { release(g); return fail(DFQ_ECUDA, "%s: %s", #x, cudaGetErrorString(e_)); } } while (0)
+    G_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    G_CUDA(cudaEventCreate(&g->ev0));
+    G_CUDA(cudaEventCreate(&g->ev1));
+    G_TRY(dev_alloc(&g->offsets, (size_t)n + 1));
+    G_TRY(dev_alloc(&g->cols, (size_t)e + kColsPad));
+    const cudaMemcpyKind kind = dev_in ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    G_CUDA(cudaMemcpyAsync(g->offsets, offsets, sizeof(int32_t) * ((size_t)n + 1), kind, g->stream));
+    if (e > 0) G_CUDA(cudaMemcpyAsync(g->cols, cols, sizeof(int32_t) * (size_t)e, kind, g->stream));
+    G_CUDA(cudaMemsetAsync(g->cols + e, 0, sizeof(int32_t) * kColsPad, g->stream));
+
+    g->bitmap_words = (int)(((int64_t)n + 31) / 32);
+    G_TRY(dev_alloc(&g->bitmap, ((size_t)g->bitmap_words + 31) & ~(size_t)31));
+    G_TRY(dev_alloc(&g->levels_tmp, (size_t)n));
+    g->large_cap = (int)std::min<int64_t>((int64_t)n, e / kMinLargeDegree + 1) + 1;
+    g->piece_cap = (int)std::min<int64_t>((int64_t)1 << 30, e / kMinPiece + g->large_cap + 2);
+    for (int i = 0; i < 2; ++i) {
+        G_TRY(dev_alloc(&g->ovf[i], (size_t)n));
+        G_TRY(dev_alloc(&g->ovfv[i], (size_t)n));
+        G_TRY(dev_alloc(&g->large[i], (size_t)g->large_cap));
+        G_TRY(dev_alloc(&g->piece_owner[i], (size_t)g->piece_cap));
+    }
+    G_TRY(dev_alloc(&g->ctl, 1));
+    G_CUDA(cudaMallocHost((void**)&g->ctl_host, sizeof(dfqk::Control)));
+    memset(g->ctl_host, 0, sizeof(dfqk::Control));
+
+    if (dev_in) {
+        int* bad = nullptr;
+        G_TRY(dev_alloc(&bad, 1));
+        cudaMemsetAsync(bad, 0, sizeof(int), g->stream);
+        validate_csr_kernel<<<g->sms * 4, 256, 0, g->stream>>>(g->offsets, g->cols, n, e, bad);
+        int hbad = 0;
+        cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+        cudaError_t e2 = cudaStreamSynchronize(g->stream);
+        cudaFree(bad);
+        if (e2 != cudaSuccess) { release(g); return fail(DFQ_ECUDA, "CSR validation: %s", cudaGetErrorString(e2)); }
+        if (hbad) {
+            release(g);
+            return fail(DFQ_EFORMAT, hbad == 1 ? "offsets decrease" : hbad == 2 ? "offsets[0] != 0 or offsets[n] != e"
+                                                                                  : "a column index is outside [0,n)");
+        }
+    }
+    G_TRY(apply_persist(g));
+    G_CUDA(cudaStreamSynchronize(g->stream));
+#undef G_TRY
+#undef G_CUDA
+    *out = g;
+    return DFQ_OK;
+}
+
+int dfq_graph_destroy(dfq_graph* g) {
+    clear_error();
+    if (!g) return fail(DFQ_EINVAL, "dfq_graph_destroy: null graph");
+    release(g);
+    return DFQ_OK;
+}
+
+int dfq_graph_get_opts(const dfq_graph* g, dfq_opts* o) {
+    clear_error();
+    if (!g || !o) return fail(DFQ_EINVAL, "dfq_graph_get_opts: null argument");
+    *o = g->opts;
+    return DFQ_OK;
+}
+
+int dfq_graph_set_opts(dfq_graph* g, const dfq_opts* o) {
+    clear_error();
+    if (!g || !o) return fail(DFQ_EINVAL, "dfq_graph_set_opts: null argument");
+    dfq_opts v = *o;
+    if (v.block_threads == 0) v.block_threads = 512;
+    if (v.local_queue_cap == 0) v.local_queue_cap = 1024;
+    if (v.timeout_ms == 0) v.timeout_ms = 5000;
+    int rc = validate_opts(v);
+    if (rc) return rc;
+    DeviceGuard dg(g->device);
+    g->opts = v;
+    return apply_persist(g);
+}
+
+void* dfq_graph_stream(dfq_graph* g) { return g ? (void*)g->stream : nullptr; }
+
+int32_t dfq_graph_num_vertices(const dfq_graph* g) { return g ? g->n : -1; }
+int64_t dfq_graph_num_edges(const dfq_graph* g) { return g ? g->e : -1; }
+
+int dfq_bfs_launch(dfq_graph* g, int32_t src, int32_t* levels_dev, int32_t* parents_dev) {
+    clear_error();
+    if (!g || !levels_dev) return fail(DFQ_EINVAL, "dfq_bfs_launch: null argument");
+    if (src < 0 || src >= g->n) return fail(DFQ_EINVAL, "source %d outside [0,%d)", src, g->n);
+    DeviceGuard dg(g->device);
+    return launch_bfs(g, src, levels_dev, parents_dev);
+}
+
+int dfq_graph_sync(dfq_graph* g) {
+    clear_error();
+    if (!g) return fail(DFQ_EINVAL, "dfq_graph_sync: null graph");
+    DeviceGuard dg(g->device);
+    return fill_stats(g, nullptr);
+}
+
+int dfq_bfs_last_stats(dfq_graph* g, dfq_stats* st) {
+    clear_error();
+    if (!g || !st) return fail(DFQ_EINVAL, "dfq_bfs_last_stats: null argument");
+    DeviceGuard dg(g->device);
+    memset(st, 0, sizeof *st);
+    return fill_stats(g, st);
+}
+
+int dfq_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, dfq_stats* stats) {
+    clear_error();
+    if (!g || !levels) return fail(DFQ_EINVAL, "dfq_bfs: graph and levels are required");
+    if (src < 0 || src >= g->n) return fail(DFQ_EINVAL, "source %d outside [0,%d)", src, g->n);
+    DeviceGuard dg(g->device);
+    const bool lv_dev = is_device_ptr(levels);
+    const bool pa_dev = parents && is_device_ptr(parents);
+    int32_t* dl = lv_dev ? levels : g->levels_tmp;
+    int32_t* dp = nullptr;
+    if (parents) {
+        if (pa_dev) dp = parents;
+        else {
+            if (!g->parents_tmp) {
+                int rc = dev_alloc(&g->parents_tmp, (size_t)g->n);
+                if (rc) return rc;
+            }
+            dp = g->parents_tmp;
+        }
+    }
+    CUDA_TRY(cudaEventRecord(g->ev0, g->stream));
+    int rc = launch_bfs(g, src, dl, dp);
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(g->ev1, g->stream));
+    if (!lv_dev)
+        CUDA_TRY(cudaMemcpyAsync(levels, dl, sizeof(int32_t) * (size_t)g->n, cudaMemcpyDeviceToHost, g->stream));
+    if (parents && !pa_dev)
+        CUDA_TRY(cudaMemcpyAsync(parents, dp, sizeof(int32_t) * (size_t)g->n, cudaMemcpyDeviceToHost, g->stream));
+    dfq_stats st;
+    memset(&st, 0, sizeof st);
+    rc = fill_stats(g, &st);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, g->ev0, g->ev1);
+    st.kernel_ms = ms;
+    if (stats) *stats = st;
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,320 @@
+"""ctypes binding of libdfq (include/dfq.h) for tests, benchmarks and scripts.
+
+Every call goes through the C ABI of dfq-bfs_gb300/lib/libdfq.so; nothing here
+computes a BFS itself.  Importing this module never needs a GPU; calls that
+launch kernels fail with DfqError when no CUDA device is present.
+
+The reference's interface for this path is the `bfs` program
+(design/shared-q/atomic-sa/our-sep/upper-bound/bfs.cu:181-317): read a graph,
+pick a source, run one cooperative launch, print Dist/Touch/Error/Time.  The
+classes below mirror those steps: `load`/generators -> `Csr`, `Graph` (device
+copy + workspace), `Graph.bfs(source)` -> levels (+ parents) and `Stats`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent.parent
+LIB_PATH = PKG / "lib" / "libdfq.so"
+
+DFQ_OK = 0
+ERRORS = {
+    -1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ETIMEOUT",
+    -5: "EFORMAT", -6: "EIO", -7: "EDEVICE", -8: "EBUSY",
+}
+CSR_SYMMETRIZE, CSR_DEDUP, CSR_NO_SELF_LOOPS = 1, 2, 4
+FMT_AUTO, FMT_SNAP, FMT_DAT, FMT_BIN = 0, 1, 2, 3
+_FORMATS = {"auto": FMT_AUTO, "snap": FMT_SNAP, "dat": FMT_DAT, "bin": FMT_BIN}
+
+# every symbol include/dfq.h declares (checked by the CPU test suite)
+EXPORTS = [
+    "dfq_last_error", "dfq_csr_load", "dfq_csr_save", "dfq_csr_from_edges", "dfq_csr_free",
+    "dfq_gen_zipf_geometric", "dfq_gen_rmat", "dfq_gen_grid", "dfq_pick_sources", "dfq_free",
+    "dfq_opts_default", "dfq_graph_create", "dfq_graph_destroy", "dfq_graph_get_opts",
+    "dfq_graph_set_opts", "dfq_graph_stream", "dfq_graph_num_vertices", "dfq_graph_num_edges",
+    "dfq_bfs", "dfq_bfs_launch", "dfq_graph_sync", "dfq_bfs_last_stats", "dfq_autotune",
+]
+
+
+class DfqError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+        self.name = ERRORS.get(code, str(code))
+
+
+class _Csr(C.Structure):
+    _fields_ = [("n", C.c_int32), ("source", C.c_int32), ("e", C.c_int64),
+                ("offsets", C.POINTER(C.c_int32)), ("cols", C.POINTER(C.c_int32))]
+
+
+class Opts(C.Structure):
+    _fields_ = [("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("medium_min_degree", C.c_int32), ("large_min_degree", C.c_int32),
+                ("local_queue_cap", C.c_int32), ("piece_edges", C.c_int32),
+                ("probe_first", C.c_int32), ("l2_persist", C.c_int32),
+                ("use_tma", C.c_int32), ("timeout_ms", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Stats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_float), ("depth", C.c_int32), ("levels", C.c_int32),
+                ("reached", C.c_int64), ("edges", C.c_int64), ("overflow", C.c_int64),
+                ("large", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libdfq.so (built by __graft_entry__.build()); raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise FileNotFoundError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+    L = C.CDLL(str(LIB_PATH))
+    P32 = C.POINTER(C.c_int32)
+    L.dfq_last_error.restype = C.c_char_p
+    L.dfq_csr_load.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.POINTER(_Csr)]
+    L.dfq_csr_save.argtypes = [C.c_char_p, C.POINTER(_Csr), C.c_int32]
+    L.dfq_csr_from_edges.argtypes = [P32, P32, C.c_int64, C.c_int32, C.c_int32, C.POINTER(_Csr)]
+    L.dfq_csr_free.argtypes = [C.POINTER(_Csr)]
+    L.dfq_csr_free.restype = None
+    L.dfq_gen_zipf_geometric.argtypes = [C.c_int32, C.c_double, C.c_double, C.c_uint64, C.POINTER(_Csr)]
+    L.dfq_gen_rmat.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                               C.c_int32, C.POINTER(_Csr)]
+    L.dfq_gen_grid.argtypes = [C.c_int32, C.c_double, C.c_uint64, C.c_int32, C.POINTER(_Csr),
+                               C.POINTER(P32)]
+    L.dfq_pick_sources.argtypes = [C.POINTER(_Csr), C.c_int32, C.c_uint64, P32]
+    L.dfq_free.argtypes = [C.c_void_p]
+    L.dfq_free.restype = None
+    L.dfq_opts_default.argtypes = [C.POINTER(Opts)]
+    L.dfq_opts_default.restype = None
+    L.dfq_graph_create.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.POINTER(Opts),
+                                   C.POINTER(C.c_void_p)]
+    L.dfq_graph_destroy.argtypes = [C.c_void_p]
+    L.dfq_graph_get_opts.argtypes = [C.c_void_p, C.POINTER(Opts)]
+    L.dfq_graph_set_opts.argtypes = [C.c_void_p, C.POINTER(Opts)]
+    L.dfq_graph_stream.argtypes = [C.c_void_p]
+    L.dfq_graph_stream.restype = C.c_void_p
+    L.dfq_graph_num_vertices.argtypes = [C.c_void_p]
+    L.dfq_graph_num_vertices.restype = C.c_int32
+    L.dfq_graph_num_edges.argtypes = [C.c_void_p]
+    L.dfq_graph_num_edges.restype = C.c_int64
+    L.dfq_bfs.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(Stats)]
+    L.dfq_bfs_launch.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+    L.dfq_graph_sync.argtypes = [C.c_void_p]
+    L.dfq_bfs_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    L.dfq_autotune.argtypes = [C.c_void_p, P32, C.c_int32, C.POINTER(Opts)]
+    for name in ("dfq_csr_load", "dfq_csr_save", "dfq_csr_from_edges", "dfq_gen_zipf_geometric",
+                 "dfq_gen_rmat", "dfq_gen_grid", "dfq_pick_sources", "dfq_graph_create",
+                 "dfq_graph_destroy", "dfq_graph_get_opts", "dfq_graph_set_opts", "dfq_bfs",
+                 "dfq_bfs_launch", "dfq_graph_sync", "dfq_bfs_last_stats", "dfq_autotune"):
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != DFQ_OK:
+        raise DfqError(rc, lib().dfq_last_error().decode(errors="replace"))
+
+
+def _p32(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Csr:
+    """Host CSR graph: offsets[n+1], cols[e] (numpy int32), source hint."""
+
+    def __init__(self, offsets: np.ndarray, cols: np.ndarray, source: int = 0, meta: dict | None = None):
+        self.offsets = np.ascontiguousarray(offsets, dtype=np.int32)
+        self.cols = np.ascontiguousarray(cols, dtype=np.int32)
+        self.source = int(source)
+        self.meta = dict(meta or {})
+
+    @property
+    def n(self) -> int:
+        return len(self.offsets) - 1
+
+    @property
+    def e(self) -> int:
+        return len(self.cols)
+
+    def degrees(self) -> np.ndarray:
+        return np.diff(self.offsets)
+
+    @classmethod
+    def _from_c(cls, c: _Csr, meta: dict | None = None) -> "Csr":
+        n, e = c.n, c.e
+        off = np.ctypeslib.as_array(c.offsets, shape=(n + 1,)).copy() if n >= 0 else np.zeros(1, np.int32)
+        cols = np.ctypeslib.as_array(c.cols, shape=(max(e, 1),))[:e].copy() if c.cols else np.zeros(0, np.int32)
+        src = c.source
+        lib().dfq_csr_free(C.byref(c))
+        return cls(off, cols, src, meta)
+
+    def _as_c(self) -> _Csr:
+        c = _Csr()
+        c.n, c.e, c.source = self.n, self.e, self.source
+        c.offsets = _p32(self.offsets)
+        c.cols = _p32(self.cols) if self.e else _p32(np.zeros(1, np.int32))
+        return c
+
+    def save(self, path: str | os.PathLike, fmt: str = "snap") -> None:
+        c = self._as_c()
+        check(lib().dfq_csr_save(str(path).encode(), C.byref(c), _FORMATS[fmt]))
+
+    def pick_sources(self, k: int, seed: int) -> np.ndarray:
+        out = np.zeros(k, np.int32)
+        c = self._as_c()
+        check(lib().dfq_pick_sources(C.byref(c), k, seed, _p32(out)))
+        return out
+
+
+def load(path: str | os.PathLike, fmt: str = "auto", flags: int = 0) -> Csr:
+    c = _Csr()
+    check(lib().dfq_csr_load(str(path).encode(), _FORMATS[fmt], flags, C.byref(c)))
+    return Csr._from_c(c, {"path": str(path)})
+
+
+def from_edges(src, dst, n: int, flags: int = 0) -> Csr:
+    s = np.ascontiguousarray(src, dtype=np.int32)
+    d = np.ascontiguousarray(dst, dtype=np.int32)
+    if len(s) != len(d):
+        raise ValueError("src and dst lengths differ")
+    c = _Csr()
+    z = np.zeros(1, np.int32)
+    check(lib().dfq_csr_from_edges(_p32(s if len(s) else z), _p32(d if len(d) else z), len(s), n, flags,
+                                   C.byref(c)))
+    return Csr._from_c(c)
+
+
+def gen_zipf_geometric(n: int, mean_deg: float = 4.7, alpha: float = 2.1, seed: int = 1) -> Csr:
+    c = _Csr()
+    check(lib().dfq_gen_zipf_geometric(n, mean_deg, alpha, seed, C.byref(c)))
+    return Csr._from_c(c, {"generator": "zipf_geometric", "n": n, "mean_deg": mean_deg, "alpha": alpha,
+                           "seed": seed})
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1, flags: int = CSR_SYMMETRIZE | CSR_DEDUP | CSR_NO_SELF_LOOPS) -> Csr:
+    cs = _Csr()
+    check(lib().dfq_gen_rmat(scale, edge_factor, a, b, c, seed, flags, C.byref(cs)))
+    return Csr._from_c(cs, {"generator": "rmat", "scale": scale, "edge_factor": edge_factor,
+                            "abc": [a, b, c], "seed": seed, "flags": flags})
+
+
+def gen_grid(side: int, delete_frac: float = 0.01, seed: int = 1, keep_lcc: bool = True):
+    """Returns (Csr, orig_ids) where orig_ids[v] is v's row-major id in the full grid."""
+    cs = _Csr()
+    ids = C.POINTER(C.c_int32)()
+    check(lib().dfq_gen_grid(side, delete_frac, seed, int(keep_lcc), C.byref(cs), C.byref(ids)))
+    n = cs.n
+    orig = np.ctypeslib.as_array(ids, shape=(max(n, 1),))[:n].copy()
+    lib().dfq_free(ids)
+    return Csr._from_c(cs, {"generator": "grid", "side": side, "delete_frac": delete_frac, "seed": seed,
+                            "keep_lcc": keep_lcc}), orig
+
+
+def default_opts() -> Opts:
+    o = Opts()
+    lib().dfq_opts_default(C.byref(o))
+    return o
+
+
+def _ptr(x) -> int:
+    """Address of a numpy array or a torch tensor (host or device)."""
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    return int(x.data_ptr())
+
+
+class Graph:
+    """Device-resident graph with its BFS workspace (dfq_graph_create)."""
+
+    def __init__(self, csr_or_offsets, cols=None, n: int | None = None, e: int | None = None,
+                 opts: Opts | None = None):
+        if isinstance(csr_or_offsets, Csr):
+            csr = csr_or_offsets
+            self._keep = (csr.offsets, csr.cols if csr.e else np.zeros(1, np.int32))
+            off_p, col_p, n, e = _ptr(csr.offsets), _ptr(self._keep[1]), csr.n, csr.e
+        else:  # device tensors / arrays with explicit sizes
+            self._keep = (csr_or_offsets, cols)
+            off_p, col_p = _ptr(csr_or_offsets), _ptr(cols)
+        h = C.c_void_p()
+        check(lib().dfq_graph_create(off_p, col_p, n, e, C.byref(opts) if opts is not None else None,
+                                     C.byref(h)))
+        self.h = h
+        self.n, self.e = n, e
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            check(lib().dfq_graph_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self) -> int:
+        return lib().dfq_graph_stream(self.h) or 0
+
+    def opts(self) -> Opts:
+        o = Opts()
+        check(lib().dfq_graph_get_opts(self.h, C.byref(o)))
+        return o
+
+    def set_opts(self, o: Opts | dict) -> None:
+        if isinstance(o, dict):
+            base = self.opts()
+            for k, v in o.items():
+                setattr(base, k, v)
+            o = base
+        check(lib().dfq_graph_set_opts(self.h, C.byref(o)))
+
+    def bfs(self, source: int, parents: bool = False, levels_out=None, parents_out=None):
+        """Synchronous BFS.  Returns (levels, parents or None, Stats).  Outputs go
+        to the given arrays/tensors (host or device) or to new numpy arrays."""
+        lv = levels_out if levels_out is not None else np.empty(self.n, np.int32)
+        pa = parents_out if parents_out is not None else (np.empty(self.n, np.int32) if parents else None)
+        st = Stats()
+        check(lib().dfq_bfs(self.h, int(source), _ptr(lv), _ptr(pa) if pa is not None else None,
+                            C.byref(st)))
+        return lv, pa, st
+
+    def launch(self, source: int, levels_dev, parents_dev=None) -> None:
+        check(lib().dfq_bfs_launch(self.h, int(source), _ptr(levels_dev),
+                                   _ptr(parents_dev) if parents_dev is not None else None))
+
+    def sync(self) -> None:
+        check(lib().dfq_graph_sync(self.h))
+
+    def last_stats(self) -> Stats:
+        st = Stats()
+        check(lib().dfq_bfs_last_stats(self.h, C.byref(st)))
+        return st
+
+    def autotune(self, sources) -> Opts:
+        s = np.ascontiguousarray(sources, dtype=np.int32)
+        o = Opts()
+        check(lib().dfq_autotune(self.h, _p32(s), len(s), C.byref(o)))
+        return o

@@ -1,0 +1,199 @@
+/*
+ * dfq.h - C ABI of libdfq, a GB300 (sm_103a) decentralized-frontier-queue BFS.
+ *
+ * This is the drop-in boundary for the reference `bfs` programs of DFQ-BFS.
+ * Each reference program is one CUDA file with a host main() and one
+ * cooperative kernel; the canonical one is
+ *   design/shared-q/atomic-sa/our-sep/upper-bound/bfs.cu   (called "DFQ" below)
+ * Every entry point below says which part of that file it replaces.
+ *
+ * Conventions
+ *   - Plain C types only: int32_t vertex ids, int64_t edge counts, caller-owned
+ *     buffers.  No exceptions cross the ABI; every function returns an int status
+ *     (DFQ_OK or a negative DFQ_E* code) and dfq_last_error() gives a message
+ *     (thread-local).
+ *   - Levels are int32 with -1 for unreached vertices: the same bit pattern as the
+ *     reference's `short cost[]` (-1 = unvisited, DFQ:192,216) widened so that
+ *     depth is not capped at 32767.
+ *   - One call in flight per dfq_graph handle (each handle owns a CUDA stream);
+ *     calls on different handles may come from different host threads.
+ */
+#ifndef DFQ_H
+#define DFQ_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define DFQ_OK          0
+#define DFQ_EINVAL     (-1)  /* bad argument (null pointer, source out of range, ...) */
+#define DFQ_ENOMEM     (-2)  /* host or device allocation failed / over budget */
+#define DFQ_ECUDA      (-3)  /* a CUDA runtime call failed */
+#define DFQ_ETIMEOUT   (-4)  /* a bounded device-side wait expired; the kernel returned */
+#define DFQ_EFORMAT    (-5)  /* malformed graph file or inconsistent CSR */
+#define DFQ_EIO        (-6)  /* file could not be opened / read / written */
+#define DFQ_EDEVICE    (-7)  /* device-side consistency check failed (queue capacity, ...) */
+#define DFQ_EBUSY      (-8)  /* no free slot / memory budget for the request */
+
+/* Message for the last failing call on this host thread ("" if none). */
+const char* dfq_last_error(void);
+
+/* ------------------------------------------------------------- host CSR */
+/*
+ * Compressed sparse rows: offsets[n+1], cols[e].  Arrays are owned by the
+ * library (malloc) and released with dfq_csr_free().  `source` is the source
+ * vertex named by the file (the reference's .dat header, DFQ:188), else 0.
+ *
+ * Replaces the reference's `Node{int start; int length}` AoS plus `int edge[]`
+ * (DFQ:38-42,190-199): SoA offsets are half the bytes per frontier vertex and
+ * need no second array to be kept consistent.
+ */
+typedef struct dfq_csr {
+    int32_t  n;        /* vertices */
+    int32_t  source;   /* source named by the input, or 0 */
+    int64_t  e;        /* directed edges (< 2^31) */
+    int32_t* offsets;  /* n+1 entries, offsets[0]=0, non-decreasing */
+    int32_t* cols;     /* e entries, each in [0,n) */
+} dfq_csr;
+
+/* dfq_csr_from_edges / dfq_csr_load flags */
+#define DFQ_CSR_SYMMETRIZE     1  /* add v->u for every u->v */
+#define DFQ_CSR_DEDUP          2  /* sort each row and drop repeated neighbours */
+#define DFQ_CSR_NO_SELF_LOOPS  4  /* drop u->u */
+
+/* file formats */
+#define DFQ_FMT_AUTO  0  /* sniff: '#' first -> SNAP, "DFQCSR01" magic -> BIN, else DAT */
+#define DFQ_FMT_SNAP  1  /* "# Nodes: N Edges: E" / "# FromNodeId ToNodeId" / "u v" lines */
+#define DFQ_FMT_DAT   2  /* reference input: "N E SOURCE", N x "start length", E x "dst x" */
+#define DFQ_FMT_BIN   3  /* binary CSR cache written by dfq_csr_save */
+
+/* Read a graph file.  Replaces the reference loader (DFQ:184-200) and adds the
+ * SNAP edge list that the reference README documents (README.md:19-32) but no
+ * reference binary reads.  SNAP edges are kept as given (directed) unless
+ * flags ask otherwise; ids >= the header's N grow N to max id + 1. */
+int dfq_csr_load(const char* path, int32_t format, int32_t flags, dfq_csr* out);
+
+/* Write a graph as SNAP text, reference .dat text, or binary CSR. */
+int dfq_csr_save(const char* path, const dfq_csr* g, int32_t format);
+
+/* Build CSR from an edge list (stable counting sort by source; file order of
+ * neighbours is kept unless DFQ_CSR_DEDUP sorts rows). */
+int dfq_csr_from_edges(const int32_t* src, const int32_t* dst, int64_t m,
+                       int32_t n, int32_t flags, dfq_csr* out);
+
+/* Release arrays owned by a dfq_csr and zero it. */
+void dfq_csr_free(dfq_csr* g);
+
+/* ------------------------------------------------------ seeded generators */
+/* All generators are deterministic in their seed and independent of the
+ * number of host threads used.  No reference counterpart: the reference's
+ * SNAP datasets are not in its repository, these stand in for them. */
+
+/* Directed graph: out-degree ~ Geometric(mean mean_deg) on {0,1,...},
+ * destinations ~ Zipf(alpha) over a seeded permutation of the ids, self-loops
+ * and repeats redrawn (so the edge count keeps its expectation). */
+int dfq_gen_zipf_geometric(int32_t n, double mean_deg, double alpha, uint64_t seed,
+                           dfq_csr* out);
+
+/* R-MAT (Chakrabarti et al. 2004): 2^scale vertices, edge_factor * 2^scale
+ * generated edges, quadrant probabilities a, b, c (d = 1-a-b-c), random vertex
+ * relabelling; flags as for dfq_csr_from_edges (usually SYMMETRIZE|DEDUP|NO_SELF_LOOPS). */
+int dfq_gen_rmat(int32_t scale, int32_t edge_factor, double a, double b, double c,
+                 uint64_t seed, int32_t flags, dfq_csr* out);
+
+/* side x side 4-neighbour grid, a seeded fraction of undirected edges deleted;
+ * if keep_lcc, only the largest connected component is kept, relabelled
+ * compactly in row-major order (orig_ids, if non-null, receives for each new
+ * vertex its row-major id in the full grid; caller frees with dfq_free). */
+int dfq_gen_grid(int32_t side, double delete_frac, uint64_t seed, int32_t keep_lcc,
+                 dfq_csr* out, int32_t** orig_ids);
+
+/* k sources drawn uniformly (seeded) from vertices with out-degree > 0. */
+int dfq_pick_sources(const dfq_csr* g, int32_t k, uint64_t seed, int32_t* out);
+
+/* free() for arrays returned by this library. */
+void dfq_free(void* p);
+
+/* ------------------------------------------------------------- device BFS */
+typedef struct dfq_opts {
+    int32_t block_threads;      /* threads per block: 256, 512 or 1024 (0 = 512) */
+    int32_t blocks_per_sm;      /* 0 = the occupancy limit (cooperative launch) */
+    int32_t medium_min_degree;  /* deg >= this leaves the small bin (block-gathered edges)
+                                   for the medium bin (one warp per vertex, int4 loads) */
+    int32_t large_min_degree;   /* deg >= this goes to the grid-wide large bin */
+    int32_t local_queue_cap;    /* per-block shared-memory frontier slots (0 = default) */
+    int32_t piece_edges;        /* large-bin piece size in edges (multiple of 64) */
+    int32_t probe_first;        /* 1: read the visited bitmap before the atomic claim */
+    int32_t l2_persist;         /* 1: visited bitmap in an L2 persisting access window */
+    int32_t use_tma;            /* 1: stage large-bin pieces into smem with cp.async.bulk */
+    int32_t timeout_ms;         /* bound on every device-side wait (0 = 5000) */
+} dfq_opts;
+
+typedef struct dfq_stats {
+    float   kernel_ms;   /* device time of the BFS launch (CUDA events, launch included:
+                            the reference's "- Time" definition, DFQ:279-288) */
+    int32_t depth;       /* largest level reached (reference "- Dist", DFQ:290-297) */
+    int32_t levels;      /* level iterations the kernel ran */
+    int64_t reached;     /* vertices with level >= 0 (reference "- Touch" numerator) */
+    int64_t edges;       /* E_R: sum of out-degrees over reached vertices */
+    int64_t overflow;    /* frontier entries that overflowed the shared-memory queues */
+    int64_t large;       /* vertices expanded through the large bin */
+} dfq_stats;
+
+typedef struct dfq_graph dfq_graph;
+
+/* Defaults for every dfq_opts field. */
+void dfq_opts_default(dfq_opts* o);
+
+/* Copy a CSR (host or device pointers) into a device-resident graph with its
+ * per-query workspace.  Replaces DFQ:194-199 + DFQ:273-277 (managed allocation
+ * and prefetch of node/edge/cost) and the static __device__ queues DFQ:96-97.
+ * opts may be null (defaults). */
+int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int64_t e,
+                     const dfq_opts* opts, dfq_graph** out);
+
+/* Release a graph and its workspace.  Replaces DFQ:312-316. */
+int dfq_graph_destroy(dfq_graph* g);
+
+/* Options in force on a graph / replace them (validated). */
+int dfq_graph_get_opts(const dfq_graph* g, dfq_opts* o);
+int dfq_graph_set_opts(dfq_graph* g, const dfq_opts* o);
+
+/* The CUDA stream a graph's launches are queued on (as void*). */
+void* dfq_graph_stream(dfq_graph* g);
+
+/* Vertex / edge counts of a graph (-1 for a null handle).  The reference
+ * keeps them in *NUM_NODES / NUM_EDGES (DFQ:185-188). */
+int32_t dfq_graph_num_vertices(const dfq_graph* g);
+int64_t dfq_graph_num_edges(const dfq_graph* g);
+
+/* Single-source BFS, synchronous.  Replaces the kernel launch and its timing
+ * (DFQ:255-288: occupancy-sized cooperative launch of CUDA_BFS_KERNEL_CG_NEW,
+ * events around launch + synchronize).  levels[n] (required) and parents[n]
+ * (nullable) may be host or device pointers; parents[src] = src, parents of
+ * unreached vertices = -1.  stats may be null. */
+int dfq_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, dfq_stats* stats);
+
+/* Queue the same BFS on the graph's stream and return at once (device
+ * pointers only).  For timing loops and CUDA-graph capture; read the outcome
+ * later with dfq_graph_sync + dfq_bfs_last_stats. */
+int dfq_bfs_launch(dfq_graph* g, int32_t src, int32_t* levels_dev, int32_t* parents_dev);
+
+/* Wait for the graph's stream; returns the device status of the last launch. */
+int dfq_graph_sync(dfq_graph* g);
+
+/* Counters of the last completed launch on this graph (kernel_ms = 0 here). */
+int dfq_bfs_last_stats(dfq_graph* g, dfq_stats* stats);
+
+/* Choose opts for this graph by timing candidate settings on a few sources;
+ * writes the winner to *best and installs it on the graph. */
+int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, dfq_opts* best);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DFQ_H */

@@ -1,0 +1,230 @@
+"""GPU parity: levels from the DFQ kernel (through the C ABI) equal the CPU
+oracle bit for bit; parents form a BFS tree; statistics match E_R.
+
+Covers the bins and queues of the kernel: degrees on every bin boundary,
+forced shared-queue overflow, the large bin with and without TMA staging,
+every block size, host and device output buffers, repeated runs, and the
+full-size configurations through size-independent properties."""
+import numpy as np
+import pytest
+
+import dfqbfs as d
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def run_and_check(g, src, opts=None, parents=True, graph=None):
+    own = graph is None
+    dg = graph or d.Graph(g, opts=opts)
+    try:
+        if opts is not None and not own:
+            dg.set_opts(opts)
+        lv, pa, st = dg.bfs(src, parents=parents)
+    finally:
+        if own:
+            dg.close()
+    want = oracle.bfs(g.offsets, g.cols, src)
+    cmp = oracle.compare(want, lv)
+    assert cmp["mismatches"] == 0, cmp
+    if parents:
+        bad = oracle.validate_tree(g.offsets, g.cols, src, lv, pa)
+        assert bad == 0, f"parent tree invalid at vertex {bad - 1}"
+    assert st.edges == oracle.reached_edges(g.offsets, want)
+    assert st.reached == int((want >= 0).sum())
+    assert st.depth == int(want.max())
+    return lv, st
+
+
+def opts(**kw):
+    o = d.default_opts()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return d.gen_zipf_geometric(262144, 4.7, 2.1, seed=1)
+
+
+def test_config1_zipf_geometric_source0(c1):
+    run_and_check(c1, 0)
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_random_small_graphs(seed):
+    rng = np.random.default_rng(1000 + seed)
+    n = int(rng.integers(1, 4097))
+    kind = seed % 3
+    if kind == 0:  # uniform random directed
+        m = int(rng.integers(0, 8 * n + 1))
+        g = d.from_edges(rng.integers(0, n, m), rng.integers(0, n, m), n)
+    elif kind == 1:  # a few hubs with degrees across the bin boundaries
+        src, dst = [], []
+        for h in range(min(n, 6)):
+            k = int(min(n, rng.choice([8, 9, 31, 32, 33, 64, 65, 1023, 1024, 1025, 2048, 4096])))
+            src += [h] * k
+            dst += rng.choice(n, size=k, replace=False).tolist()
+        m = 3 * n
+        src += rng.integers(0, n, m).tolist()
+        dst += rng.integers(0, n, m).tolist()
+        g = d.from_edges(src, dst, n, d.CSR_SYMMETRIZE | d.CSR_DEDUP)
+    else:
+        side = max(1, int(np.sqrt(n)))
+        g, _ = d.gen_grid(side, float(rng.uniform(0, 0.3)), seed=seed)
+    src = int(rng.integers(0, g.n))
+    run_and_check(g, src)
+
+
+BOUNDARY_DEGS = [1, 2, 3, 4, 5, 7, 8, 9, 31, 32, 33, 63, 64, 65, 127, 128, 1023, 1024, 1025, 2047, 2048,
+                 2049, 4095, 4096, 4097, 16384, 16385]
+
+
+@pytest.fixture(scope="module")
+def boundary_graph():
+    rng = np.random.default_rng(7)
+    n = 40000
+    src, dst = [], []
+    for i, k in enumerate(BOUNDARY_DEGS):
+        src += [i] * k
+        dst += rng.choice(n, size=k, replace=False).tolist()
+    # chain the hubs so one BFS reaches all of them at different levels
+    src += list(range(len(BOUNDARY_DEGS) - 1))
+    dst += list(range(1, len(BOUNDARY_DEGS)))
+    m = 60000
+    src += rng.integers(0, n, m).tolist()
+    dst += rng.integers(0, n, m).tolist()
+    return d.from_edges(src, dst, n, d.CSR_DEDUP)
+
+
+@pytest.mark.parametrize("B", [256, 512, 1024])
+@pytest.mark.parametrize("tma", [0, 1])
+@pytest.mark.parametrize("probe", [0, 1])
+def test_boundaries_all_block_sizes(boundary_graph, B, tma, probe):
+    run_and_check(boundary_graph, 0, opts(block_threads=B, use_tma=tma, probe_first=probe))
+
+
+@pytest.mark.parametrize("medium,large,piece", [
+    (1, 32, 64),          # everything medium or large, tiny pieces
+    (1 << 30, 1 << 30, 2048),  # no medium, no large: all block-gathered
+    (8, 64, 128),
+    (32, 1024, 4096),
+    (64, 16384, 16384),
+])
+def test_bin_thresholds(boundary_graph, medium, large, piece):
+    run_and_check(boundary_graph, 0, opts(medium_min_degree=medium, large_min_degree=large, piece_edges=piece))
+
+
+@pytest.mark.parametrize("cap", [1, 16, 100])
+def test_forced_overflow(cap):
+    g = d.gen_rmat(14, 16, seed=3)
+    src = int(g.pick_sources(1, seed=3)[0])
+    _, st = run_and_check(g, src, opts(local_queue_cap=cap))
+    assert st.overflow > 0
+
+
+def test_large_bin_used():
+    g = d.gen_rmat(16, 16, seed=4)
+    src = int(g.pick_sources(1, seed=4)[0])
+    _, st = run_and_check(g, src, opts(large_min_degree=256, piece_edges=256))
+    assert st.large > 0
+
+
+def test_grid_high_diameter():
+    g, _ = d.gen_grid(512, 0.01, seed=5)
+    lv, st = run_and_check(g, 0)
+    assert st.depth > 1000
+
+
+def test_rmat18_several_sources():
+    g = d.gen_rmat(18, 16, seed=6)
+    with d.Graph(g) as dg:
+        for s in g.pick_sources(4, seed=6):
+            run_and_check(g, int(s), graph=dg)
+
+
+def test_repeated_runs_identical():
+    g = d.gen_rmat(15, 16, seed=8)
+    src = int(g.pick_sources(1, seed=8)[0])
+    with d.Graph(g) as dg:
+        first, _, _ = dg.bfs(src)
+        first = first.copy()
+        for _ in range(20):
+            lv, _, _ = dg.bfs(src)
+            assert np.array_equal(lv, first)
+    assert oracle.compare(oracle.bfs(g.offsets, g.cols, src), first)["mismatches"] == 0
+
+
+def test_device_buffers_and_launch_api():
+    torch = pytest.importorskip("torch")
+    g = d.gen_rmat(14, 8, seed=9)
+    src = int(g.pick_sources(1, seed=9)[0])
+    off = torch.from_numpy(g.offsets).cuda()
+    cols = torch.from_numpy(g.cols).cuda()
+    with d.Graph(off, cols, n=g.n, e=g.e) as dg:  # device-pointer CSR input
+        lv = torch.empty(g.n, dtype=torch.int32, device="cuda")
+        pa = torch.empty(g.n, dtype=torch.int32, device="cuda")
+        dg.bfs(src, levels_out=lv, parents_out=pa)
+        want = oracle.bfs(g.offsets, g.cols, src)
+        assert oracle.compare(want, lv.cpu().numpy())["mismatches"] == 0
+        assert oracle.validate_tree(g.offsets, g.cols, src, lv.cpu().numpy(), pa.cpu().numpy()) == 0
+        lv2 = torch.full((g.n,), 7, dtype=torch.int32, device="cuda")
+        dg.launch(src, lv2)
+        dg.sync()
+        assert torch.equal(lv, lv2)
+        st = dg.last_stats()
+        assert st.edges == oracle.reached_edges(g.offsets, want)
+
+
+def test_invalid_source_and_csr():
+    g = d.gen_rmat(8, 4, seed=1)
+    with d.Graph(g) as dg:
+        with pytest.raises(d.DfqError) as e:
+            dg.bfs(g.n)
+        assert e.value.name == "EINVAL"
+        with pytest.raises(d.DfqError):
+            dg.set_opts(opts(block_threads=300))
+    bad = d.Csr(g.offsets.copy(), g.cols.copy())
+    bad.cols[0] = g.n + 5
+    with pytest.raises(d.DfqError) as e:
+        d.Graph(bad)
+    assert e.value.name == "EFORMAT"
+    torch = pytest.importorskip("torch")
+    off = torch.from_numpy(g.offsets).cuda()
+    cols = torch.from_numpy(bad.cols).cuda()
+    with pytest.raises(d.DfqError) as e:
+        d.Graph(off, cols, n=g.n, e=g.e)
+    assert e.value.name == "EFORMAT"
+
+
+def test_single_vertex_and_empty_graph():
+    g = d.from_edges([], [], 1)
+    run_and_check(g, 0)
+    g = d.from_edges([], [], 50)
+    run_and_check(g, 13)
+
+
+def test_autotune_keeps_parity():
+    g = d.gen_rmat(15, 16, seed=10)
+    srcs = g.pick_sources(2, seed=10)
+    with d.Graph(g) as dg:
+        best = dg.autotune(srcs)
+        assert best.block_threads in (256, 512, 1024)
+        for s in srcs:
+            run_and_check(g, int(s), graph=dg)
+
+
+@pytest.mark.parametrize("cfg", ["rmat22", "grid4096"])
+def test_full_size_configs(cfg):
+    """Full-size RMAT-22 (config 2) and 4096^2 grid (config 3): bit-exact
+    against the oracle for a few sources."""
+    if cfg == "rmat22":
+        g = d.gen_rmat(22, 16, seed=1)
+        srcs = g.pick_sources(64, seed=1)[:2]
+    else:
+        g, orig = d.gen_grid(4096, 0.01, seed=1)
+        srcs = [0, g.n - 1]
+    with d.Graph(g) as dg:
+        for s in srcs:
+            run_and_check(g, int(s), graph=dg, parents=(cfg == "rmat22"))
