@@ -37,6 +37,7 @@ EXPORTS = [
     "dfq_opts_default", "dfq_graph_create", "dfq_graph_destroy", "dfq_graph_get_opts",
     "dfq_graph_set_opts", "dfq_graph_stream", "dfq_graph_num_vertices", "dfq_graph_num_edges",
     "dfq_bfs", "dfq_bfs_launch", "dfq_graph_sync", "dfq_bfs_last_stats", "dfq_autotune",
+    "dfq_bfs_noalloc",
 ]
 
 
@@ -116,10 +117,13 @@ def lib() -> C.CDLL:
     L.dfq_graph_sync.argtypes = [C.c_void_p]
     L.dfq_bfs_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     L.dfq_autotune.argtypes = [C.c_void_p, P32, C.c_int32, C.POINTER(Opts)]
+    L.dfq_bfs_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_int32, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.POINTER(Stats)]
     for name in ("dfq_csr_load", "dfq_csr_save", "dfq_csr_from_edges", "dfq_gen_zipf_geometric",
                  "dfq_gen_rmat", "dfq_gen_grid", "dfq_pick_sources", "dfq_graph_create",
                  "dfq_graph_destroy", "dfq_graph_get_opts", "dfq_graph_set_opts", "dfq_bfs",
-                 "dfq_bfs_launch", "dfq_graph_sync", "dfq_bfs_last_stats", "dfq_autotune"):
+                 "dfq_bfs_launch", "dfq_graph_sync", "dfq_bfs_last_stats", "dfq_autotune",
+                 "dfq_bfs_noalloc"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -318,3 +322,17 @@ class Graph:
         o = Opts()
         check(lib().dfq_autotune(self.h, _p32(s), len(s), C.byref(o)))
         return o
+
+
+NOALLOC_SCRATCH_BYTES = 32 << 20
+
+
+def bfs_noalloc(offsets_dev, cols_dev, n: int, e: int, source: int, levels_dev, parents_dev=None,
+                stream: int = 0) -> Stats:
+    """dfq_bfs_noalloc: BFS over caller-owned device buffers with the library's
+    fixed scratch array (no allocation).  Returns the Stats (kernel_ms = 0)."""
+    st = Stats()
+    check(lib().dfq_bfs_noalloc(_ptr(offsets_dev), _ptr(cols_dev), int(n), int(e), int(source),
+                                _ptr(levels_dev), _ptr(parents_dev) if parents_dev is not None else None,
+                                stream or None, C.byref(st)))
+    return st

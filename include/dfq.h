@@ -193,6 +193,37 @@ int dfq_bfs_last_stats(dfq_graph* g, dfq_stats* stats);
  * writes the winner to *best and installs it on the graph. */
 int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, dfq_opts* best);
 
+/* -------------------------------------------------- allocation-free BFS */
+/* No counterpart in the reference (its kernel uses static __device__ queues
+ * plus managed allocations made by main()).
+ *
+ * For callers that cannot call cudaMalloc: a host framework that owns the
+ * GPU's memory through its own pool, a serving process that reserves its HBM
+ * budget at start-up and forbids later allocation, or code that cannot accept
+ * cudaMalloc/cudaFree stalling every stream on the device.  dfq_graph_create
+ * allocates a workspace per graph; this entry point allocates nothing.  The
+ * caller passes the CSR (offsets[n+1], cols[e]) and levels[n] (parents[n]
+ * nullable) in device memory it owns; the kernel's scratch (visited bitmap,
+ * frontier queues, control block) is one fixed array of
+ * DFQ_NOALLOC_SCRATCH_BYTES inside libdfq that every GPU loading the library
+ * holds until the process exits.  That bounds the graph to roughly
+ * n * 24 bytes plus (e/2048 + e/1024) * 20 bytes of scratch (about 1.3 million
+ * vertices); larger graphs are rejected with DFQ_ENOMEM and a message naming
+ * the bytes needed.  cols must be 16-byte aligned.  The CSR is checked on the
+ * device first (DFQ_EFORMAT if malformed).
+ *
+ * Runs on `stream` (null = the legacy default stream) with the default
+ * dfq_opts and returns after the BFS has finished; stats (nullable) gets the
+ * counters, kernel_ms = 0 (no events are created).  The first call on a device
+ * looks up the scratch array's device address and caches it: make it before
+ * any stream capture.  All calls share the one array: calls that overlap on
+ * the GPU (other streams, other host threads) race and must be serialised by
+ * the caller. */
+#define DFQ_NOALLOC_SCRATCH_BYTES (32u << 20)
+int dfq_bfs_noalloc(const int32_t* offsets_dev, const int32_t* cols_dev, int32_t n, int64_t e,
+                    int32_t src, int32_t* levels_dev, int32_t* parents_dev, void* stream,
+                    dfq_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif
