@@ -57,15 +57,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def load_graph():
+def load_graph(scale: int = 22):
     import dfqbfs as d
-    cache = Path(os.environ.get("DFQ_BENCH_CACHE", "/tmp")) / "dfq_rmat22_ef16_s1.bin"
+    cache = Path(os.environ.get("DFQ_BENCH_CACHE", "/tmp")) / f"dfq_rmat{scale}_ef16_s1.bin"
     if cache.exists():
         try:
             return d.load(cache, "bin")
         except d.DfqError:
             pass
-    g = d.gen_rmat(22, 16, 0.57, 0.19, 0.19, seed=1)
+    g = d.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed=1)
     try:
         g.save(cache, "bin")
     except d.DfqError:
@@ -205,15 +205,109 @@ def run_reference(args, ws, rank, pg):
     return 0
 
 
+def grid_sources(orig, side: int, k_interior: int = 12, seed: int = 1):
+    """Config-3 sources: the 4 corners of the full grid (nearest kept vertex if
+    a corner left the largest component) and k seeded interior vertices."""
+    pos = {int(f): i for i, f in enumerate(orig)} if len(orig) < 1 << 22 else None
+    lookup = (lambda f: pos.get(f)) if pos is not None else (
+        lambda f: (lambda j: int(j) if j < len(orig) and orig[j] == f else None)(np.searchsorted(orig, f)))
+    out = []
+    for r0, c0 in [(0, 0), (0, side - 1), (side - 1, 0), (side - 1, side - 1)]:
+        found = None
+        for rad in range(side):
+            for dr in range(-rad, rad + 1):
+                for dc in (-(rad - abs(dr)), rad - abs(dr)):
+                    r, c = r0 + dr, c0 + dc
+                    if 0 <= r < side and 0 <= c < side:
+                        v = lookup(r * side + c)
+                        if v is not None:
+                            found = v
+                            break
+                if found is not None:
+                    break
+            if found is not None:
+                break
+        out.append(found)
+    rng = np.random.default_rng(seed)
+    interior = rng.choice(len(orig), size=k_interior, replace=False)
+    return out + [int(x) for x in interior]
+
+
+def workload_graph(name: str, scale: int):
+    import dfqbfs as d
+    if name == "rmat22":
+        g = load_graph(scale)
+        return g, g.pick_sources(64, seed=1), dict(WORKLOAD, n=g.n, e=g.e)
+    if name == "grid4096":
+        g, orig = d.gen_grid(4096, 0.01, seed=1)
+        srcs = np.array(grid_sources(orig, 4096), np.int32)
+        return g, srcs, {"workload": "grid4096_del1pct_lcc_16src", "graph": "4096x4096 4-neighbour grid, 1% of "
+                         "undirected edges deleted (seeded), largest component, row-major relabel", "seed": 1,
+                         "sources": 16, "n": g.n, "e": g.e}
+    if name == "zipf262k":
+        g = d.gen_zipf_geometric(262144, 4.7, 2.1, seed=1)
+        return g, np.array([0], np.int32), {"workload": "zipf_geometric_262144_src0", "n": g.n, "e": g.e}
+    raise SystemExit(f"unknown workload {name}")
+
+
+def measure_device(dg, srcs, n, steps, warmup, torch, with_clocks=None):
+    """Device-resident timing of `steps` passes over srcs (one launch per
+    source); returns total ms (events on the graph's stream), per-launch ms,
+    per-source E_R / |R| / levels."""
+    stream = torch.cuda.ExternalStream(dg.stream)
+    levels = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)]
+    er, rr, lvls = [], [], []
+    for s in srcs:  # untimed pass: E_R and |R| from the kernel's own counters
+        dg.launch(int(s), levels[0])
+        st = dg.last_stats()
+        er.append(st.edges)
+        rr.append(st.reached)
+        lvls.append(st.levels)
+
+    def step(evs=None):
+        for i, s in enumerate(srcs):
+            if evs is not None:
+                evs[i][0].record(stream)
+            dg.launch(int(s), levels[i & 1])
+            if evs is not None:
+                evs[i][1].record(stream)
+
+    for _ in range(warmup):
+        step()
+    dg.sync()
+    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in srcs]
+           for _ in range(steps)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    if with_clocks is not None:
+        with_clocks.__enter__()
+    t0.record(stream)
+    for k in range(steps):
+        step(evs[k])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    if with_clocks is not None:
+        with_clocks.__exit__(None, None, None)
+    dg.sync()
+    launch_ms = np.array([[a.elapsed_time(b) for (a, b) in row] for row in evs])
+    return {"ms_total": t0.elapsed_time(t1), "launch_ms": launch_ms, "er": np.array(er, np.int64),
+            "rr": np.array(rr, np.int64), "levels": np.array(lvls), "levels_buf": levels}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="dfq", choices=["dfq", "reference"])
+    ap.add_argument("--workload", default="rmat22", choices=["rmat22", "grid4096", "zipf262k"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference GPU kernel")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the grid (config 3) secondary line")
     ap.add_argument("--sources", type=int, default=64)
+    ap.add_argument("--scale", type=int, default=22,
+                    help="R-MAT scale (22 is the benchmark; smaller scales are for profiler captures)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     args = ap.parse_args()
     ws, rank, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
@@ -225,51 +319,21 @@ def main():
     import dfqbfs as d
     torch.cuda.set_device(local)
     t_gen = time.perf_counter()
-    g = load_graph()
+    g, all_srcs, cfg = workload_graph(args.workload, args.scale)
     t_gen = time.perf_counter() - t_gen
-    srcs = g.pick_sources(64, seed=1)[: args.sources]
+    srcs = all_srcs[: args.sources]
     dg = d.Graph(g)
     n = g.n
-    stream = torch.cuda.ExternalStream(dg.stream)
-    levels = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)]
-
-    # per-source E_R and |R| from one untimed pass (checked against the kernel's own counters)
-    er, rr = [], []
-    for s in srcs:
-        dg.launch(int(s), levels[0])
-        st = dg.last_stats()
-        er.append(st.edges)
-        rr.append(st.reached)
-    er, rr = np.array(er, np.int64), np.array(rr, np.int64)
+    barrier(pg)
+    ck = Clocks(local)
+    m = measure_device(dg, srcs, n, args.steps, args.warmup, torch, with_clocks=ck)
+    barrier(pg)
+    er, rr = m["er"], m["rr"]
     step_edges = int(er.sum())
     step_bytes = int((4 * er + 8 * rr + 4 * n).sum())
-
-    def step(evs=None):
-        for i, s in enumerate(srcs):
-            if evs is not None:
-                evs[i][0].record(stream)
-            dg.launch(int(s), levels[i & 1])
-            if evs is not None:
-                evs[i][1].record(stream)
-
-    for _ in range(args.warmup):
-        step()
-    dg.sync()
-    evs = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in srcs]
-           for _ in range(args.steps)]
-    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier(pg)
-    torch.cuda.synchronize()
-    with Clocks(local) as ck:
-        t0.record(stream)
-        for k in range(args.steps):
-            step(evs[k])
-        t1.record(stream)
-        torch.cuda.synchronize()
-    dg.sync()
-    barrier(pg)
-    ms_total = t0.elapsed_time(t1)
-    launch_ms = [a.elapsed_time(b) for row in evs for (a, b) in row]
+    ms_total = m["ms_total"]
+    launch_ms = m["launch_ms"].ravel()
+    levels = m["levels_buf"]
     ms_max = allreduce_max(pg, ms_total)
     total_edges = allreduce_sum(pg, float(step_edges * args.steps))
     value = total_edges / (ms_max * 1e-3) / 1e9
@@ -279,57 +343,78 @@ def main():
     achieved = bytes_per_launch / (avg_launch_ms * 1e-3) / 1e9
 
     # e2e: public API with pinned host level buffers (launch + D2H inside the timed region)
-    host_lv = [torch.empty(n, dtype=torch.int32, pin_memory=True) for _ in range(2)]
-    for i, s in enumerate(srcs[:4]):
-        dg.bfs(int(s), levels_out=host_lv[i & 1])
-    e2e_steps = max(1, min(args.steps, 3))
-    barrier(pg)
-    te0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        for i, s in enumerate(srcs):
+    e2e, e2e_steps, ok_parity = None, 0, None
+    if not args.no_e2e:
+        host_lv = [torch.empty(n, dtype=torch.int32, pin_memory=True) for _ in range(2)]
+        for i, s in enumerate(srcs[:4]):
             dg.bfs(int(s), levels_out=host_lv[i & 1])
-    te = time.perf_counter() - te0
-    te = allreduce_max(pg, te)
-    e2e_edges = allreduce_sum(pg, float(step_edges * e2e_steps))
-    e2e = e2e_edges / te / 1e9
-    # parity spot check of the e2e output against the device run
-    ok_parity = bool(torch.equal(host_lv[(len(srcs) - 1) & 1], levels[(len(srcs) - 1) & 1].cpu()))
+        e2e_steps = max(1, min(args.steps, 3))
+        barrier(pg)
+        te0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for i, s in enumerate(srcs):
+                dg.bfs(int(s), levels_out=host_lv[i & 1])
+        te = time.perf_counter() - te0
+        te = allreduce_max(pg, te)
+        e2e_edges = allreduce_sum(pg, float(step_edges * e2e_steps))
+        e2e = e2e_edges / te / 1e9
+        # parity spot check of the e2e output against the device run
+        ok_parity = bool(torch.equal(host_lv[(len(srcs) - 1) & 1], levels[(len(srcs) - 1) & 1].cpu()))
 
     traffic = None
-    tp = ROOT / "profiles" / "traffic_rmat22.txt"
+    tp = ROOT / "profiles" / f"traffic_{args.workload}.txt"
     if tp.exists():
         for line in tp.read_text().splitlines():
             if line.startswith("dram_bytes_per_launch="):
                 traffic = float(line.split("=", 1)[1])
 
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+    metric = METRIC if args.workload == "rmat22" else f"BFS GTEPS ({cfg['workload']})"
+    out = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
-           "config": dict(WORKLOAD, n=n, e=g.e, parallelism=f"replicas x{ws}", opts=dg.opts().as_dict(),
+           "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
+           "config": dict(cfg, sources=len(srcs), parallelism=f"replicas x{ws}", opts=dg.opts().as_dict(),
                           edges_per_step=step_edges, gen_s=round(t_gen, 2)),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                         "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                         "kernel": "dfq_bfs_kernel", "bytes_alg_per_launch": bytes_per_launch,
                         "avg_launch_ms": avg_launch_ms},
-           "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * len(srcs),
-                   "d2h_bytes_per_step": 4 * n * len(srcs), "api": "dfq_bfs (host levels)",
-                   "steps": e2e_steps, "parity_vs_device": ok_parity},
+           "e2e": ({"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * len(srcs),
+                    "d2h_bytes_per_step": 4 * n * len(srcs), "api": "dfq_bfs (host levels)",
+                    "steps": e2e_steps, "parity_vs_device": ok_parity} if e2e is not None else None),
            "gpu_launches": args.steps * len(srcs),
            "clocks": ck.summary(),
            "per_bfs_ms_median": float(np.median(launch_ms)),
-           "gteps_median_source": float(np.median(er / (np.array(launch_ms[:len(srcs)]) * 1e-3) / 1e9))}
+           "us_per_level": float(np.median(m["launch_ms"][0] * 1e3 / np.maximum(m["levels"], 1)))}
     if rank == 0 and not args.no_cpu:
         import oracle
         oracle.lib()
         edges, tcpu, nsrc = cpu_sample(g, srcs, budget_s=15.0)
         out["cpu_baseline"] = {"value": edges / tcpu / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
-                               "sample": f"{nsrc} of the 64 sources, serial oracle BFS, {tcpu:.1f} s"}
+                               "sample": f"{nsrc} of the {len(srcs)} sources, serial oracle BFS, {tcpu:.1f} s"}
     if rank == 0 and not args.no_ref_gpu:
-        out["reference_gpu"] = reference_gpu(g, srcs)
+        out["reference_gpu"] = reference_gpu(g, srcs, max_sources=16 if args.workload == "rmat22" else 2)
     dg.close()
+    if rank == 0 and args.workload == "rmat22" and not args.no_secondary:
+        out["secondary"] = secondary_grid(torch, d, args)
     if rank == 0:
         print(json.dumps(out))
     return 0
+
+
+def secondary_grid(torch, d, args):
+    """Config 3 (high diameter): GTEPS and microseconds per level on 4 of its
+    16 sources (2 corners, 2 interior), next to the reference kernel."""
+    g, srcs, cfg = workload_graph("grid4096", 22)
+    srcs = np.array([srcs[0], srcs[3], srcs[4], srcs[5]], np.int32)
+    with d.Graph(g) as dg:
+        m = measure_device(dg, srcs, g.n, 1, 1, torch)
+    ms = m["launch_ms"][0]
+    res = {"workload": cfg["workload"], "sources": srcs.tolist(), "gteps": float(m["er"].sum() / (ms.sum() * 1e-3) / 1e9),
+           "ms_median": float(np.median(ms)), "levels_median": float(np.median(m["levels"])),
+           "us_per_level": float(np.median(ms * 1e3 / np.maximum(m["levels"], 1)))}
+    if not args.no_ref_gpu:
+        res["reference_gpu"] = reference_gpu(g, srcs[:1], max_sources=1)
+    return res
 
 
 def reference_gpu(g, srcs, max_sources=16):
@@ -356,7 +441,9 @@ def reference_gpu(g, srcs, max_sources=16):
                 errors += oracle.compare(want, lv)["near_errors"]
                 ms.append(t)
                 gteps.append(oracle.reached_edges(g.offsets, want) / (t * 1e-3) / 1e9)
+                depth = int(want.max())
             res.update({"sources": len(ms), "ms_median": float(np.median(ms)),
+                        "us_per_level_last": float(ms[-1] * 1e3 / max(depth + 1, 1)),
                         "gteps_median": float(np.median(gteps)),
                         "gteps_aggregate": float(sum(g_ * m for g_, m in zip(gteps, ms)) / sum(ms)),
                         "errors": int(errors), "grid": ref.grid})

@@ -59,9 +59,10 @@ extern "C" int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, 
         {&dfq_opts::block_threads, {256, 512, 1024}},
         {&dfq_opts::large_min_degree, {256, 512, 1024, 2048, 4096, 16384}},
         {&dfq_opts::medium_min_degree, {8, 16, 32, 64, 128, 1 << 30}},
-        {&dfq_opts::piece_edges, {1024, 2048, 4096, 8192}},
+        {&dfq_opts::piece_edges, {128, 256, 512, 1024}},
         {&dfq_opts::local_queue_cap, {256, 512, 1024, 2048}},
-        {&dfq_opts::probe_first, {0, 1}},
+        {&dfq_opts::local_edge_budget, {1024, 4096, 8192, 32768, 1 << 30}},
+        {&dfq_opts::probe_first, {0, 1, 2}},
         {&dfq_opts::use_tma, {0, 1}},
         {&dfq_opts::blocks_per_sm, {0, 1, 2}},
         {&dfq_opts::l2_persist, {0, 1}},

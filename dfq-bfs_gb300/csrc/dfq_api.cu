@@ -78,9 +78,11 @@ int validate_opts(const dfq_opts& o) {
     if (o.medium_min_degree < 1) return fail(DFQ_EINVAL, "medium_min_degree must be >= 1");
     if (o.piece_edges < kMinPiece || o.piece_edges % 64 || o.piece_edges > 16384)
         return fail(DFQ_EINVAL, "piece_edges must be a multiple of 64 in [64,16384]");
-    if (o.local_queue_cap < 0 || o.local_queue_cap > 8192)
-        return fail(DFQ_EINVAL, "local_queue_cap must be in [0,8192]");
+    if (o.local_queue_cap < 1 || o.local_queue_cap > 8192)
+        return fail(DFQ_EINVAL, "local_queue_cap must be in [1,8192]");
+    if (o.local_edge_budget < 0) return fail(DFQ_EINVAL, "local_edge_budget must be >= 0");
     if (o.timeout_ms < 1) return fail(DFQ_EINVAL, "timeout_ms must be >= 1");
+    if (o.probe_first < 0 || o.probe_first > 2) return fail(DFQ_EINVAL, "probe_first must be 0, 1 or 2");
     const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges);
     if (L.bytes > 200 * 1024)
         return fail(DFQ_EINVAL, "options need %d bytes of shared memory per block (max 204800)", L.bytes);
@@ -223,6 +225,7 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     p.large_min = o.large_min_degree;
     p.piece_edges = o.piece_edges;
     p.local_cap = o.local_queue_cap;
+    p.local_budget = o.local_edge_budget;
     p.probe_first = o.probe_first;
     p.use_tma = o.use_tma;
     p.timeout_ns = (long long)o.timeout_ms * 1000000LL;
@@ -271,10 +274,11 @@ void dfq_opts_default(dfq_opts* o) {
     o->block_threads = 512;
     o->blocks_per_sm = 0;
     o->medium_min_degree = 32;
-    o->large_min_degree = 1024;
+    o->large_min_degree = 256;
     o->local_queue_cap = 1024;
-    o->piece_edges = 2048;
-    o->probe_first = 1;
+    o->local_edge_budget = 8192;
+    o->piece_edges = 256;
+    o->probe_first = 2;
     o->l2_persist = 0;
     o->use_tma = 1;
     o->timeout_ms = 5000;
@@ -292,6 +296,7 @@ int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int
     if (opts) o = *opts;
     if (o.block_threads == 0) o.block_threads = 512;
     if (o.local_queue_cap == 0) o.local_queue_cap = 1024;
+    if (o.local_edge_budget == 0) o.local_edge_budget = 8192;
     if (o.timeout_ms == 0) o.timeout_ms = 5000;
     int rc = validate_opts(o);
     if (rc) return rc;
@@ -388,6 +393,7 @@ int dfq_graph_set_opts(dfq_graph* g, const dfq_opts* o) {
     dfq_opts v = *o;
     if (v.block_threads == 0) v.block_threads = 512;
     if (v.local_queue_cap == 0) v.local_queue_cap = 1024;
+    if (v.local_edge_budget == 0) v.local_edge_budget = 8192;
     if (v.timeout_ms == 0) v.timeout_ms = 5000;
     int rc = validate_opts(v);
     if (rc) return rc;
@@ -422,6 +428,22 @@ int dfq_bfs_last_stats(dfq_graph* g, dfq_stats* st) {
     DeviceGuard dg(g->device);
     memset(st, 0, sizeof *st);
     return fill_stats(g, st);
+}
+
+int dfq_bfs_last_trace(dfq_graph* g, int64_t* start_ns, int32_t* frontier, int32_t max_levels) {
+    clear_error();
+    if (!g || max_levels < 0 || (max_levels > 0 && (!start_ns || !frontier)))
+        return fail(DFQ_EINVAL, "dfq_bfs_last_trace: bad arguments");
+    DeviceGuard dg(g->device);
+    int rc = fill_stats(g, nullptr);
+    if (rc) return rc;
+    const dfqk::Control& c = *g->ctl_host;
+    int n = std::min(std::min(max_levels, dfqk::kTraceLevels), c.stats.levels + 1);
+    for (int i = 0; i < n; ++i) {
+        start_ns[i] = c.trace_ns[i];
+        frontier[i] = c.trace_frontier[i];
+    }
+    return n;
 }
 
 int dfq_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, dfq_stats* stats) {

@@ -12,22 +12,26 @@
 //  * Claims are atomicOr on a visited bitmap (N/8 bytes, L2-resident), so each
 //    vertex enters exactly one frontier; levels/parents are plain stores by the
 //    unique claimer.
-//  * Decentralized queues: each block keeps the frontier entries it discovered
-//    in its own shared-memory queue and expands them itself at the next level;
-//    slots are reserved once per warp (ballot/popc/shuffle).  When the block's
-//    queue is full the excess goes to a global overflow queue that all blocks
-//    share with dynamic chunking.
+//  * Decentralized queues: each block keeps frontier entries it discovered in
+//    its own shared-memory queue and expands them itself at the next level.
+//    A warp reserves slots once for all its lanes, all-or-nothing against the
+//    queue's entry capacity and edge budget (one 64-bit CAS on count|degrees);
+//    a batch that does not fit goes to the global overflow queue, which all
+//    warps of the grid drain with dynamic chunks.
 //  * Degree bins (the reference's "our-sep" bins, bfs.cu:16-36,119-123):
-//      small  [1, medium_min)      -> block-wide load-balanced gather (prefix sum
-//                                     of degrees + binary search: no idle lanes)
+//      small  [1, medium_min)      -> warp-level load-balanced gather (prefix sum
+//                                     of 32 degrees + binary search: no idle lanes)
 //      medium [medium_min, large)  -> one warp per vertex, int4 column loads
-//      large  [large_min, inf)     -> global large queue, split into fixed pieces
-//                                     that every block pulls; each piece is staged
-//                                     into shared memory by cp.async.bulk (TMA)
-//  * One grid barrier per level (bounded spin, error word on timeout) instead of
-//    three grid.sync() calls (bfs.cu:114,170,177); termination is decided from
-//    a counter that every block reads after the barrier, so all blocks leave
-//    together (the reference's racy `*done` flag, bfs.cu:115, is gone).
+//      large  [large_min, inf)     -> global large queue cut into fixed pieces;
+//                                     every warp pulls pieces and stages each one
+//                                     into its shared-memory buffer with
+//                                     cp.async.bulk (TMA), double-buffered
+//  * Warps work independently inside a level (no block barrier until the level
+//    ends), so a slow warp only delays itself.  One grid barrier per level
+//    (bounded spin, error word on timeout) instead of three grid.sync() calls
+//    (bfs.cu:114,170,177); termination is decided from a counter every block
+//    reads after the barrier, so all blocks leave together (the reference's
+//    racy `*done` flag, bfs.cu:115, is gone).
 //
 // Every queue is sized so it cannot overflow (a vertex is claimed once per
 // BFS), and every index is still checked before the store; a violated bound
@@ -44,14 +48,18 @@ constexpr unsigned kFull = 0xffffffffu;
 enum : int { kErrNone = 0, kErrBarrierTimeout = 1, kErrTmaTimeout = 2, kErrQueueCap = 3 };
 
 // Counters of one level's output frontier.  Rotated over three slots: level L
-// reads lv[L%3], appends to lv[(L+1)%3] and clears lv[(L+2)%3].
-struct LevelCtr {
+// reads lv[L%3], appends to lv[(L+1)%3] and clears lv[(L+2)%3].  Producer
+// counters and the two consumer cursors sit on separate 128-byte lines so
+// atomics on one do not queue behind atomics on another.
+struct alignas(128) LevelCtr {
     int ovf_count;                  // entries in the global overflow queue
-    int ovf_grab;                   // chunk cursor over that queue
-    int large_grab;                 // piece cursor over the large queue
     int pushed;                     // frontier entries (local + overflow + large)
     unsigned long long large_pack;  // (large entries << 32) | pieces
-    int pad[2];
+    int pad0[28];
+    int ovf_grab;                   // chunk cursor over the overflow queue
+    int pad1[31];
+    int large_grab;                 // piece cursor over the large queue
+    int pad2[31];
 };
 
 struct DevStats {
@@ -64,18 +72,23 @@ struct DevStats {
     int pad[2];
 };
 
+constexpr int kTraceLevels = 64;  // levels with a recorded start time / frontier size
+
 // Per-launch control block; zeroed by the host before every launch.
 struct Control {
     LevelCtr lv[3];
-    unsigned barrier;  // grid barrier arrivals (monotone within a launch)
+    alignas(128) unsigned barrier;  // grid barrier arrivals (monotone within a launch)
+    int pad_b[31];
     int status;        // first error (kErr*)
     int err_info[2];
     DevStats stats;
+    long long trace_ns[kTraceLevels];   // %globaltimer when level L starts (block 0)
+    int trace_frontier[kTraceLevels];   // frontier entries of level L
 };
 
 struct Params {
     const int* __restrict__ offsets;  // n+1
-    const int* __restrict__ cols;     // e, padded by >= 16 entries
+    const int* __restrict__ cols;     // e; reads stay inside 16-byte chunks holding a valid entry
     int n;
     int src;
     int* levels;
@@ -91,8 +104,9 @@ struct Params {
     Control* ctl;
     int medium_min;
     int large_min;
-    int piece_edges;  // multiple of 64
-    int local_cap;
+    int piece_edges;  // per-warp piece, multiple of 64
+    int local_cap;    // local queue entries
+    int local_budget; // local queue edges
     int probe_first;
     int use_tma;
     long long timeout_ns;
@@ -108,6 +122,12 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
+}
+__device__ __forceinline__ void red_add_release(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 __device__ __forceinline__ int4 ldg4(const int* p) { return __ldg(reinterpret_cast<const int4*>(p)); }
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
@@ -163,18 +183,22 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
     }
 }
 
-// Grid barrier over all co-resident blocks of a cooperative launch.  One
-// arrival per block on a monotone counter, then a bounded acquire-spin until
-// every block of this phase has arrived.  Returns false (all threads of the
-// block) if the wait timed out or another block reported an error.
+// Grid barrier over all co-resident blocks of a cooperative launch.  After the
+// block barrier, thread 0 arrives with one release-ordered reduction on a
+// monotone counter (release is cumulative over the block's writes it observed
+// through the block barrier, so no separate fence is needed) and polls the
+// counter with acquire loads until every block of this phase has arrived,
+// bounded by timeout_ns.  Thread 0 then reads the counters of the level that
+// starts (`next`) into s_in, so the rest of the block never loads them from
+// global memory.  Returns false (all threads of the block) if the wait timed
+// out or another block reported an error.
 __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, long long timeout_ns,
-                                             int* s_flag) {
+                                             int* s_flag, const LevelCtr* next, int* s_in) {
     __syncthreads();
     if (threadIdx.x == 0) {
         target += gridDim.x;
         int ok = 1;
-        __threadfence();
-        atomicAdd(&ctl->barrier, 1u);
+        red_add_release(&ctl->barrier, 1u);
         unsigned long long t0 = 0;
         for (unsigned it = 0;; ++it) {
             unsigned cur = ld_acquire(&ctl->barrier);
@@ -190,9 +214,15 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
                 }
             }
         }
-        __threadfence();
         if (ok && *(volatile int*)&ctl->status != 0) ok = 0;
         *s_flag = ok;
+        if (ok) {
+            s_in[0] = __ldcg(&next->pushed);
+            s_in[1] = __ldcg(&next->ovf_count);
+            const unsigned long long lp = __ldcg(&next->large_pack);
+            s_in[2] = (int)(lp >> 32);
+            s_in[3] = (int)(unsigned)lp;
+        }
     }
     __syncthreads();
     return *s_flag != 0;
@@ -200,72 +230,78 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
 
 // ------------------------------------------------------------ shared layout
 struct SmemLayout {
-    int q_off;      // local queues: 2 buffers x {start, deg, v} x cap ints
-    int st_off;     // chunk staging: {start, deg, v} x B ints
-    int scan_off;   // B ints
-    int mlist_off;  // B ints
-    int tma_off;    // 2 x (piece + 16) ints, 128-byte aligned
-    int bar_off;    // 2 x u64
+    int q_off;    // local queues: 2 buffers x {start, deg, v} x cap ints
+    int wl_off;   // per-warp gather scratch: {scan, start, parent} x 32 ints
+    int tma_off;  // per-warp piece buffers: 2 x (piece + 16) ints, 128-byte aligned
+    int bar_off;  // per-warp mbarriers: 2 x u64
     int bytes;
 };
 __host__ __device__ inline SmemLayout smem_layout(int B, int cap, int piece) {
     SmemLayout L;
+    const int NW = B / 32;
     int o = 0;
-    L.q_off = o;     o += 2 * 3 * cap * 4;
-    L.st_off = o;    o += 3 * B * 4;
-    L.scan_off = o;  o += B * 4;
-    L.mlist_off = o; o += B * 4;
+    L.q_off = o;    o += 2 * 3 * cap * 4;
+    L.wl_off = o;   o += NW * 3 * 32 * 4;
     o = (o + 127) & ~127;
-    L.tma_off = o;   o += 2 * (piece + 16) * 4;
+    L.tma_off = o;  o += NW * 2 * (piece + 16) * 4;
     o = (o + 15) & ~15;
-    L.bar_off = o;   o += 16;
+    L.bar_off = o;  o += NW * 2 * 8;
     L.bytes = o;
     return L;
 }
 
-// ------------------------------------------------------------ per-level context
-template <bool PAR>
-struct Ctx {
-    const int* __restrict__ offsets;
-    const int* __restrict__ cols;
-    int* levels;
-    int* parents;
-    unsigned* bitmap;
-    // next-level outputs
-    int2* ovf_out;
-    int* ovfv_out;
-    int4* large_out;
-    int* piece_owner_out;
-    LevelCtr* cout;
-    int* qn_start;
-    int* qn_deg;
-    int* qn_v;
-    int* s_cnt_next;
-    int* s_ovf_pushed;
-    int* s_large_pushed;
-    int* s_claimed;
-    Control* ctl;
-    int cap;
-    int n;
-    int large_cap;
-    int piece_cap;
-    int lvl_next;
-    int large_min;
-    int piece_edges;
-    int probe_first;
-    // per-thread statistics
-    unsigned long long edges;
-    unsigned long long claims;
+
+// ------------------------------------------------------------ block state
+// Shared scalars of the running block.  Device functions name them directly
+// (static shared addresses cost no registers), and read the launch
+// parameters from the parameter bank, so the per-edge code keeps few values
+// live across the level loop.
+struct BlockShared {
+    unsigned long long local_pack;  // (entries << 32) | edges of the next local queue
+    int cnt_cur;                    // entries of the local queue being expanded
+    int local_grab;                 // cursor over it (32 entries per warp grab)
+    int ovf_pushed;                 // entries this block sent to the overflow queue
+    int large_pushed;               // entries this block sent to the large queue
+    int claimed;                    // this block claimed a vertex at this level
+    int flag;                       // barrier verdict
+    int in[4];                      // this level's input: pushed, overflow, large entries, pieces
+    int depth;                      // deepest level this block claimed into
+    unsigned long long overflow;    // entries this block sent to the overflow queue (whole BFS)
+    unsigned long long large;       // entries this block sent to the large queue (whole BFS)
+    unsigned long long red[2];
+};
+static __shared__ BlockShared sh;
+extern __shared__ __align__(128) unsigned char dfq_smem[];
+
+// Uniform per-level values.
+struct Lv {
+    int next;   // level being written (L + 1)
+    int out;    // parity of the output queues (L + 1) & 1
+    int cslot;  // counter slot of the output frontier (L + 1) % 3
+    int qn;     // local queue buffer being filled
+    int cap;    // entries this block may keep locally at this level
+    int probe;  // probe the bitmap before claiming
 };
 
-// Push up to four claimed vertices per lane into the block's next local queue;
-// whatever does not fit goes to the global overflow queue.  Warp-collective:
-// every lane of the warp must call it (with loc == 0 if it has nothing).
+// Per-thread tallies (32-bit: one thread never scans 2^32 edges, e < 2^31).
+struct Tally {
+    unsigned edges;
+    unsigned claims;
+};
+
+// Push up to four claimed vertices per lane into the block's next local
+// queue, all-or-nothing per warp against its entry limit and edge budget;
+// a batch that does not fit goes to the global overflow queue.
+// Warp-collective: every lane calls it (loc == 0 if it has nothing).
 template <bool PAR>
-__device__ __forceinline__ void push_local(Ctx<PAR>& c, unsigned loc, const int (&st)[4],
+__device__ __forceinline__ void push_local(const Params& p, const Lv& lv, unsigned loc, const int (&st)[4],
                                            const int (&dg)[4], const int (&v)[4]) {
     const int lane = threadIdx.x & 31;
     const int cnt = __popc(loc);
+    int dsum = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (loc >> j & 1) dsum += dg[j];
     int incl = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -274,78 +310,109 @@ __device__ __forceinline__ void push_local(Ctx<PAR>& c, unsigned loc, const int 
     }
     const int tot = __shfl_sync(kFull, incl, 31);
     if (tot == 0) return;
-    int base = 0;
-    if (lane == 0) base = atomicAdd(c.s_cnt_next, tot);
-    base = __shfl_sync(kFull, base, 0);
-    const int ofirst = base > c.cap ? base : c.cap;
-    const int ocnt = base + tot - ofirst;
-    int gbase = 0;
-    if (ocnt > 0) {
-        if (lane == 0) {
-            gbase = atomicAdd(&c.cout->ovf_count, ocnt);
-            atomicAdd(c.s_ovf_pushed, ocnt);
-        }
-        gbase = __shfl_sync(kFull, gbase, 0);
-    }
-    int pos = base + incl - cnt;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        if (loc >> j & 1) {
-            if (pos < c.cap) {
-                c.qn_start[pos] = st[j];
-                c.qn_deg[pos] = dg[j];
-                if (PAR) c.qn_v[pos] = v[j];
-            } else {
-                const int gi = gbase + (pos - ofirst);
-                if (gi < c.n) {
-                    c.ovf_out[gi] = make_int2(st[j], dg[j]);
-                    if (PAR) c.ovfv_out[gi] = v[j];
-                } else {
-                    set_error(c.ctl, kErrQueueCap, gi, c.n);
-                }
+    for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(kFull, dsum, o);
+    int base = -1, gbase = 0;
+    if (lane == 0) {
+        unsigned long long old = *(volatile unsigned long long*)&sh.local_pack;
+        while (true) {
+            const unsigned n_ent = (unsigned)(old >> 32), n_deg = (unsigned)old;
+            if (n_ent + (unsigned)tot > (unsigned)lv.cap || n_deg + (unsigned)dsum > (unsigned)p.local_budget) break;
+            const unsigned long long want =
+                ((unsigned long long)(n_ent + tot) << 32) | (unsigned long long)(n_deg + (unsigned)dsum);
+            const unsigned long long seen = atomicCAS(&sh.local_pack, old, want);
+            if (seen == old) { base = (int)n_ent; break; }
+            old = seen;
+        }
+        if (base < 0) {
+            gbase = atomicAdd(&p.ctl->lv[lv.cslot].ovf_count, tot);
+            atomicAdd(&sh.ovf_pushed, tot);
+        }
+    }
+    base = __shfl_sync(kFull, base, 0);
+    int pos = incl - cnt;
+    if (base >= 0) {
+        int* qs = reinterpret_cast<int*>(dfq_smem) + lv.qn * 3 * p.local_cap;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (loc >> j & 1) {
+                qs[base + pos] = st[j];
+                qs[p.local_cap + base + pos] = dg[j];
+                if (PAR) qs[2 * p.local_cap + base + pos] = v[j];
+                ++pos;
             }
-            ++pos;
+        }
+    } else {
+        gbase = __shfl_sync(kFull, gbase, 0);
+        int2* ovf = lv.out ? p.ovf[1] : p.ovf[0];
+        int* ovfv = lv.out ? p.ovfv[1] : p.ovfv[0];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (loc >> j & 1) {
+                const int gi = gbase + pos;
+                if (gi < p.n) {
+                    ovf[gi] = make_int2(st[j], dg[j]);
+                    if (PAR) ovfv[gi] = v[j];
+                } else {
+                    set_error(p.ctl, kErrQueueCap, gi, p.n);
+                }
+                ++pos;
+            }
         }
     }
 }
 
-template <bool PAR>
-__device__ __forceinline__ void push_large(Ctx<PAR>& c, int st, int dg, int v) {
-    const unsigned np = (unsigned)((dg + c.piece_edges - 1) / c.piece_edges);
-    unsigned long long old = atomicAdd(&c.cout->large_pack, (1ull << 32) | np);
+__device__ __forceinline__ void push_large(const Params& p, const Lv& lv, int st, int dg, int v) {
+    const unsigned np = (unsigned)((dg + p.piece_edges - 1) / p.piece_edges);
+    unsigned long long old = atomicAdd(&p.ctl->lv[lv.cslot].large_pack, (1ull << 32) | np);
     const int slot = (int)(old >> 32);
     const unsigned poff = (unsigned)old;
-    atomicAdd(c.s_large_pushed, 1);
-    if (slot >= c.large_cap || poff + np > (unsigned)c.piece_cap) {
-        set_error(c.ctl, kErrQueueCap, slot, (int)poff);
+    atomicAdd(&sh.large_pushed, 1);
+    if (slot >= p.large_cap || poff + np > (unsigned)p.piece_cap) {
+        set_error(p.ctl, kErrQueueCap, slot, (int)poff);
         return;
     }
-    c.large_out[slot] = make_int4(st, dg, (int)poff, v);
-    for (unsigned i = 0; i < np; ++i) c.piece_owner_out[poff + i] = slot;
+    (lv.out ? p.large[1] : p.large[0])[slot] = make_int4(st, dg, (int)poff, v);
+    int* owner = lv.out ? p.piece_owner[1] : p.piece_owner[0];
+    for (unsigned i = 0; i < np; ++i) owner[poff + i] = slot;
 }
 
 // Scan up to four neighbours per lane: probe, claim, record, push.
 // Warp-collective (calls push_local).
 template <bool PAR>
-__device__ __forceinline__ void visit4(Ctx<PAR>& c, const int (&v)[4], unsigned vmask,
+__device__ __forceinline__ void visit4(const Params& p, const Lv& lv, Tally& t, const int (&v)[4], unsigned vmask,
                                        const int (&par)[4]) {
     unsigned claim = 0;
+    int so[4], eo[4];  // offsets[v], offsets[v+1]
+    if (!lv.probe) {
+        // small frontier: latency, not atomic traffic, bounds the level, so
+        // every candidate's row bounds are loaded alongside its atomicOr
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            so[j] = 0;
+            eo[j] = 0;
+            if (vmask >> j & 1) {
+                so[j] = __ldg(p.offsets + v[j]);
+                eo[j] = __ldg(p.offsets + v[j] + 1);
+            }
+        }
+    }
     if (vmask) {
         unsigned w[4] = {0u, 0u, 0u, 0u};
-        if (c.probe_first) {
+        if (lv.probe) {
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                if (vmask >> j & 1) w[j] = c.bitmap[v[j] >> 5];
+                if (vmask >> j & 1) w[j] = p.bitmap[v[j] >> 5];
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const unsigned bit = 1u << (v[j] & 31);
             if ((vmask >> j & 1) && !(w[j] & bit)) {
-                const unsigned old = atomicOr(&c.bitmap[v[j] >> 5], bit);
+                const unsigned old = atomicOr(&p.bitmap[v[j] >> 5], bit);
                 if (!(old & bit)) claim |= 1u << j;
             }
         }
-        c.edges += __popc(vmask);
+        t.edges += __popc(vmask);
     }
     int st[4], dg[4];
     unsigned loc = 0;
@@ -354,139 +421,125 @@ __device__ __forceinline__ void visit4(Ctx<PAR>& c, const int (&v)[4], unsigned 
         st[j] = 0;
         dg[j] = 0;
         if (claim >> j & 1) {
-            c.levels[v[j]] = c.lvl_next;
-            if (PAR) c.parents[v[j]] = par[j];
-            st[j] = __ldg(c.offsets + v[j]);
-            dg[j] = __ldg(c.offsets + v[j] + 1) - st[j];
+            p.levels[v[j]] = lv.next;
+            if (PAR) p.parents[v[j]] = par[j];
+            if (lv.probe) {
+                st[j] = __ldg(p.offsets + v[j]);
+                dg[j] = __ldg(p.offsets + v[j] + 1) - st[j];
+            } else {
+                st[j] = so[j];
+                dg[j] = eo[j] - so[j];
+                // small frontier: pull the row this vertex will expand at the
+                // next level into L2 now, off the next level's critical path
+                if (dg[j] > 0) {
+                    prefetch_l2(p.cols + st[j]);
+                    if (dg[j] > 32) prefetch_l2(p.cols + st[j] + dg[j] - 1);
+                }
+            }
         }
     }
     if (claim) {
-        c.claims += __popc(claim);
-        *c.s_claimed = 1;
+        t.claims += __popc(claim);
+        sh.claimed = 1;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             if (!(claim >> j & 1) || dg[j] == 0) continue;
-            if (dg[j] >= c.large_min) push_large(c, st[j], dg[j], v[j]);
+            if (dg[j] >= p.large_min) push_large(p, lv, st[j], dg[j], v[j]);
             else loc |= 1u << j;
         }
     }
-    push_local(c, loc, st, dg, v);
+    push_local<PAR>(p, lv, loc, st, dg, v);
 }
 
-// One warp expands one medium vertex: int4 column loads from the 16-byte
-// aligned floor of its list; lanes mask what lies outside [e0, e1).
+// One warp expands one list [s, s+d): int4 column loads from the 16-byte
+// aligned floor of the list; lanes mask what lies outside it.
 template <bool PAR>
-__device__ __forceinline__ void warp_expand(Ctx<PAR>& c, int s, int d, int u) {
+__device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally& t, int s, int d, int u) {
     const int lane = threadIdx.x & 31;
-    const int e0 = s, e1 = s + d, a0 = e0 & ~3;
+    const int e0 = s, e1 = s + d;
     const int par[4] = {u, u, u, u};
-    for (int base = a0; base < e1; base += 128) {
+    for (int base = e0 & ~3; base < e1; base += 128) {
         const int k4 = base + lane * 4;
         int4 x = make_int4(0, 0, 0, 0);
         unsigned vm = 0;
         if (k4 < e1) {
-            x = ldg4(c.cols + k4);
+            x = ldg4(p.cols + k4);
 #pragma unroll
             for (int j = 0; j < 4; ++j)
                 if (k4 + j >= e0 && k4 + j < e1) vm |= 1u << j;
         }
         const int v[4] = {x.x, x.y, x.z, x.w};
-        visit4(c, v, vm, par);
+        visit4<PAR>(p, lv, t, v, vm, par);
     }
 }
 
-// Expand m (<= B) frontier entries held in shared memory: medium entries one
-// warp each, small entries by a block-wide load-balanced gather.
-// Block-collective; ends with __syncthreads.
-template <int B, bool PAR>
-__device__ __forceinline__ void process_entries(Ctx<PAR>& c, const int* es, const int* ed,
-                                                const int* ev, int m, int* scan, int* mlist,
-                                                int2* s_warp, int medium_min) {
-    constexpr int NW = B / 32;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int d = tid < m ? ed[tid] : 0;
-    const int med = d >= medium_min ? 1 : 0;
+// Expand one frontier entry per lane (has == false: no entry).  Medium
+// entries one at a time with the whole warp; small entries by a warp-level
+// gather over the concatenation of their lists (4 edges per lane per round).
+// wl: this warp's 96-int scratch (scan, start, parent).  Warp-collective.
+template <bool PAR>
+__device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tally& t, int* wl, bool has, int s,
+                                             int d, int u) {
+    const int lane = threadIdx.x & 31;
+    if (!has) d = 0;
+    const bool med = d >= p.medium_min;
+    unsigned mmask = __ballot_sync(kFull, med);
+    while (mmask) {
+        const int i = __ffs(mmask) - 1;
+        mmask &= mmask - 1;
+        warp_expand<PAR>(p, lv, t, __shfl_sync(kFull, s, i), __shfl_sync(kFull, d, i), __shfl_sync(kFull, u, i));
+    }
     const int ds = med ? 0 : d;
-    // block exclusive scan of (small degree, medium flag)
-    int x = ds, y = med;
+    int incl = ds;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int tx = __shfl_up_sync(kFull, x, o), ty = __shfl_up_sync(kFull, y, o);
-        if (lane >= o) { x += tx; y += ty; }
+        int tt = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += tt;
     }
-    if (lane == 31) s_warp[warp] = make_int2(x, y);
-    __syncthreads();
-    if (warp == 0) {
-        int2 w = lane < NW ? s_warp[lane] : make_int2(0, 0);
-        int wx = w.x, wy = w.y;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int tx = __shfl_up_sync(kFull, wx, o), ty = __shfl_up_sync(kFull, wy, o);
-            if (lane >= o) { wx += tx; wy += ty; }
-        }
-        if (lane < NW) s_warp[lane] = make_int2(wx, wy);
-    }
-    __syncthreads();
-    const int2 pre = warp > 0 ? s_warp[warp - 1] : make_int2(0, 0);
-    const int2 tot = s_warp[NW - 1];
-    scan[tid] = pre.x + x - ds;
-    if (med) mlist[pre.y + y - 1] = tid;
-    __syncthreads();
-    // medium: one warp per vertex
-    for (int j = warp; j < tot.y; j += NW) {
-        const int i = mlist[j];
-        warp_expand(c, es[i], ed[i], PAR ? ev[i] : 0);
-    }
-    // small: 4 edges per thread per round, owner by binary search over scan
-    const int T = tot.x;
-    for (int base = 0; base < T; base += 4 * B) {
+    const int T = __shfl_sync(kFull, incl, 31);
+    if (T == 0) return;
+    __syncwarp();
+    wl[lane] = incl - ds;
+    wl[32 + lane] = s;
+    if (PAR) wl[64 + lane] = u;
+    __syncwarp();
+    for (int base = 0; base < T; base += 128) {
         int v[4], par[4];
         unsigned vm = 0;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const int k = base + j * B + tid;
+            const int k = base + j * 32 + lane;
             v[j] = 0;
             par[j] = 0;
             if (k < T) {
-                int lo = 0, hi = B;  // first index with scan > k
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (scan[mid] <= k) lo = mid + 1;
-                    else hi = mid;
-                }
-                const int own = lo - 1;
-                v[j] = __ldg(c.cols + es[own] + (k - scan[own]));
-                if (PAR) par[j] = ev[own];
+                // owner = largest index with scan <= k (scan[0] = 0 <= k and scan
+                // is non-decreasing, so this lands on an entry with k inside its
+                // list); steps 16+8+4+2+1 keep own + step <= 31
+                int own = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (wl[own + step] <= k) own += step;
+                v[j] = __ldg(p.cols + wl[32 + own] + (k - wl[own]));
+                if (PAR) par[j] = wl[64 + own];
                 vm |= 1u << j;
             }
         }
-        visit4(c, v, vm, par);
+        visit4<PAR>(p, lv, t, v, vm, par);
     }
-    __syncthreads();
 }
 
 template <int B, bool PAR>
-__global__ void __launch_bounds__(B) dfq_bfs_kernel(Params p) {
+__global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_constant__ Params p) {
     constexpr int NW = B / 32;
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int s_cnt_next, s_cnt_cur, s_ovf_pushed, s_large_pushed, s_claimed, s_flag;
-    __shared__ int s_bc;
-    __shared__ int s_pc[2][4];  // staged piece: {e0, count, offset in buffer, parent}
-    __shared__ int2 s_warp[NW];
-    __shared__ unsigned long long s_red[4];
-
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // grid-wide warp index, interleaved across blocks so that consecutive
+    // statically assigned chunks land on different SMs
+    const int gwarp = warp * (int)gridDim.x + (int)blockIdx.x, nwarps = (int)gridDim.x * NW;
     const SmemLayout lay = smem_layout(B, p.local_cap, p.piece_edges);
-    const int cap = p.local_cap;
-    int* qbase = reinterpret_cast<int*>(smem + lay.q_off);
-    int* st_start = reinterpret_cast<int*>(smem + lay.st_off);
-    int* st_deg = st_start + B;
-    int* st_v = st_deg + B;
-    int* scan = reinterpret_cast<int*>(smem + lay.scan_off);
-    int* mlist = reinterpret_cast<int*>(smem + lay.mlist_off);
-    int* tma_buf[2] = {reinterpret_cast<int*>(smem + lay.tma_off),
-                       reinterpret_cast<int*>(smem + lay.tma_off) + p.piece_edges + 16};
-    unsigned long long* bars = reinterpret_cast<unsigned long long*>(smem + lay.bar_off);
+    const int P = p.piece_edges;
+    int* wl = reinterpret_cast<int*>(dfq_smem + lay.wl_off) + warp * 96;
+    int* wbuf0 = reinterpret_cast<int*>(dfq_smem + lay.tma_off) + warp * 2 * (P + 16);
+    unsigned long long* wbar = reinterpret_cast<unsigned long long*>(dfq_smem + lay.bar_off) + warp * 2;
     Control* ctl = p.ctl;
 
     // ---- init: levels, parents, bitmap (source pre-set so no ordering is needed)
@@ -504,7 +557,7 @@ __global__ void __launch_bounds__(B) dfq_bfs_kernel(Params p) {
             const int s0 = p.offsets[src], d = p.offsets[src + 1] - s0;
             if (d > 0) {
                 if (d >= p.large_min) {
-                    const int np = (d + p.piece_edges - 1) / p.piece_edges;
+                    const int np = (d + P - 1) / P;
                     p.large[0][0] = make_int4(s0, d, 0, src);
                     for (int i = 0; i < np; ++i) p.piece_owner[0][i] = 0;
                     ctl->lv[0].large_pack = (1ull << 32) | (unsigned)np;
@@ -518,44 +571,33 @@ __global__ void __launch_bounds__(B) dfq_bfs_kernel(Params p) {
         }
     }
     if (tid == 0) {
-        s_cnt_next = s_cnt_cur = s_ovf_pushed = s_large_pushed = s_claimed = 0;
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        sh.local_pack = 0ull;
+        sh.cnt_cur = sh.local_grab = sh.ovf_pushed = sh.large_pushed = sh.claimed = 0;
+        sh.depth = 0;
+        sh.overflow = sh.large = 0ull;
+    }
+    if (lane == 0) {
+        mbar_init(&wbar[0], 1);
+        mbar_init(&wbar[1], 1);
         mbar_fence_init();
     }
-    unsigned phase_bits = 0;  // parity of the next completion of bars[0], bars[1]
+    unsigned phase_bits = 0;  // parity of the next completion of wbar[0], wbar[1]
     unsigned bar_target = 0;
-    unsigned long long my_overflow = 0, my_large = 0;
     int cur = 0;
     int L = 0;
+    Tally t{0u, 0u};
+    bool warp_failed = false;
 
-    Ctx<PAR> c;
-    c.offsets = p.offsets;
-    c.cols = p.cols;
-    c.levels = p.levels;
-    c.parents = p.parents;
-    c.bitmap = p.bitmap;
-    c.s_cnt_next = &s_cnt_next;
-    c.s_ovf_pushed = &s_ovf_pushed;
-    c.s_large_pushed = &s_large_pushed;
-    c.s_claimed = &s_claimed;
-    c.ctl = ctl;
-    c.cap = cap;
-    c.n = p.n;
-    c.large_cap = p.large_cap;
-    c.piece_cap = p.piece_cap;
-    c.large_min = p.large_min;
-    c.piece_edges = p.piece_edges;
-    c.probe_first = p.probe_first;
-    c.edges = 0;
-    c.claims = 0;
-
-    bool ok = grid_barrier(ctl, bar_target, p.timeout_ns, &s_flag);
+    bool ok = grid_barrier(ctl, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[0], sh.in);
 
     for (; ok; ++L) {
-        LevelCtr* cin = &ctl->lv[L % 3];
-        const int pushed = __ldcg(&cin->pushed);
+        const int pushed = sh.in[0];
+        if (blockIdx.x == 0 && tid == 0 && L < kTraceLevels) {
+            ctl->trace_ns[L] = (long long)globaltimer();
+            ctl->trace_frontier[L] = pushed;
+        }
         if (pushed == 0) break;
+        LevelCtr* cin = &ctl->lv[L % 3];
         if (blockIdx.x == 0 && tid == 0) {
             LevelCtr* cz = &ctl->lv[(L + 2) % 3];
             cz->ovf_count = 0;
@@ -564,85 +606,102 @@ __global__ void __launch_bounds__(B) dfq_bfs_kernel(Params p) {
             cz->pushed = 0;
             cz->large_pack = 0ull;
         }
-        const int in = L & 1, out = in ^ 1;
-        const int n_ovf = __ldcg(&cin->ovf_count);
-        const unsigned long long lp = __ldcg(&cin->large_pack);
-        const int total_pieces = (int)(unsigned)(lp & 0xffffffffull);
+        const int in = L & 1;
+        const int n_ovf = sh.in[1];
+        const int total_pieces = sh.in[3];
+        Lv lv;
+        lv.next = L + 1;
+        lv.out = in ^ 1;
+        lv.cslot = (L + 1) % 3;
+        lv.qn = cur ^ 1;
+        {
+            // a block keeps at most about twice its fair share of a frontier
+            // of this level's size; the rest is shared through the global queue
+            const int share = (pushed + (int)gridDim.x - 1) / (int)gridDim.x;
+            lv.cap = min(p.local_cap, max(32, 2 * share));
+        }
+        // probe the bitmap before claiming only where many edges hit visited
+        // vertices (large frontiers); 2 = decide per level
+        lv.probe = p.probe_first == 2 ? (pushed >= 8 * nwarps ? 1 : 0) : p.probe_first;
 
-        c.ovf_out = p.ovf[out];
-        c.ovfv_out = p.ovfv[out];
-        c.large_out = p.large[out];
-        c.piece_owner_out = p.piece_owner[out];
-        c.cout = &ctl->lv[(L + 1) % 3];
-        c.qn_start = qbase + (cur ^ 1) * 3 * cap;
-        c.qn_deg = c.qn_start + cap;
-        c.qn_v = c.qn_deg + cap;
-        c.lvl_next = L + 1;
-        const int* qc_start = qbase + cur * 3 * cap;
-        const int* qc_deg = qc_start + cap;
-        const int* qc_v = qc_deg + cap;
-
-        // (1) this block's own queue from the previous level
-        const int nloc = s_cnt_cur;
-        for (int b0 = 0; b0 < nloc; b0 += B) {
-            const int m = nloc - b0 < B ? nloc - b0 : B;
-            process_entries<B, PAR>(c, qc_start + b0, qc_deg + b0, qc_v + b0, m, scan, mlist, s_warp,
-                                    p.medium_min);
+        // (1) this block's own queue from the previous level, 32 entries per grab
+        {
+            const int nloc = sh.cnt_cur;
+            const int* qc = reinterpret_cast<const int*>(dfq_smem) + cur * 3 * p.local_cap;
+            while (true) {
+                int j = 0;
+                if (lane == 0) j = atomicAdd(&sh.local_grab, 32);
+                j = __shfl_sync(kFull, j, 0);
+                if (j >= nloc) break;
+                const int i = j + lane;
+                const bool has = i < nloc;
+                warp_process<PAR>(p, lv, t, wl, has, has ? qc[i] : 0, has ? qc[p.local_cap + i] : 0,
+                                  (PAR && has) ? qc[2 * p.local_cap + i] : 0);
+            }
         }
 
-        // (2) large pieces, double-buffered: the next piece's copy is in flight
-        //     while the current one is expanded
-        if (total_pieces > 0) {
+        // (2) large pieces: each warp pulls pieces and double-buffers their
+        //     bulk copies into its own shared-memory buffers.  Schedule: when
+        //     there are no more pieces than warps each piece goes to one warp;
+        //     otherwise the first 3/4 go round-robin and the rest are pulled
+        //     from a counter
+        if (total_pieces > 0 && !warp_failed) {
             const int4* large_in = p.large[in];
             const int* owner_in = p.piece_owner[in];
-            const int P = p.piece_edges;
-            auto fetch = [&](int b) {  // thread 0 only
-                const int g = atomicAdd(&cin->large_grab, 1);
-                if (g >= total_pieces) { s_pc[b][1] = -1; return; }
+            const int p_static = total_pieces <= nwarps ? total_pieces : total_pieces - total_pieces / 4;
+            int s_next = gwarp;
+            int m_e0 = 0, m_cnt = -1, m_off = 0, m_par = 0;  // lane 0: next piece
+            auto fetch = [&](int b) {  // lane 0 only
+                int g;
+                if (s_next < p_static) { g = s_next; s_next += nwarps; }
+                else if (p_static < total_pieces) g = p_static + atomicAdd(&cin->large_grab, 1);
+                else g = total_pieces;
+                if (g >= total_pieces) { m_cnt = -1; return; }
                 const int slot = __ldcg(owner_in + g);
                 const int4 ent = __ldcg(large_in + slot);
                 const int e0 = ent.x + (g - ent.z) * P;
                 const int e1 = min(e0 + P, ent.x + ent.y);
                 const int a0 = e0 & ~3, a1 = (e1 + 3) & ~3;
-                s_pc[b][0] = e0;
-                s_pc[b][1] = e1 - e0;
-                s_pc[b][2] = e0 - a0;
-                s_pc[b][3] = ent.w;
+                m_e0 = e0;
+                m_cnt = e1 - e0;
+                m_off = e0 - a0;
+                m_par = ent.w;
                 if (p.use_tma) {
+                    int* dst = wbuf0 + b * (P + 16);
                     const unsigned bytes = (unsigned)(a1 - a0) * 4u;
-                    mbar_arrive_expect_tx(&bars[b], bytes);
-                    tma_load_1d(tma_buf[b], p.cols + a0, bytes, &bars[b]);
+                    mbar_arrive_expect_tx(&wbar[b], bytes);
+                    tma_load_1d(dst, p.cols + a0, bytes, &wbar[b]);
                 }
             };
-            if (tid == 0) fetch(0);
-            __syncthreads();
+            if (lane == 0) fetch(0);
             int cb = 0;
             while (true) {
-                const int cnt = s_pc[cb][1];
+                const int cnt = __shfl_sync(kFull, m_cnt, 0);
                 if (cnt < 0) break;
-                const int e0 = s_pc[cb][0], off = s_pc[cb][2], par0 = s_pc[cb][3];
-                if (tid == 0) fetch(cb ^ 1);
+                const int e0 = __shfl_sync(kFull, m_e0, 0);
+                const int off = __shfl_sync(kFull, m_off, 0);
+                const int par0 = __shfl_sync(kFull, m_par, 0);
+                if (lane == 0) fetch(cb ^ 1);
                 const int par[4] = {par0, par0, par0, par0};
                 if (p.use_tma) {
-                    const bool landed = mbar_wait_bounded(&bars[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
-                    if (__syncthreads_or(!landed)) {
+                    const bool landed = mbar_wait_bounded(&wbar[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
+                    if (__any_sync(kFull, !landed)) {
                         // never expand a buffer whose copy did not land: record the
-                        // error, give both copies of this block one more bounded
-                        // wait, and leave the level (the barrier then stops the grid)
-                        if (tid == 0) {
+                        // error, give this warp's copies one more bounded wait, stop
+                        if (lane == 0) {
                             set_error(ctl, kErrTmaTimeout, (int)blockIdx.x, e0);
-                            mbar_wait_bounded(&bars[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
-                            if (s_pc[cb ^ 1][1] >= 0)
-                                mbar_wait_bounded(&bars[cb ^ 1], (phase_bits >> (cb ^ 1)) & 1u, p.timeout_ns);
+                            mbar_wait_bounded(&wbar[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
+                            if (m_cnt >= 0)
+                                mbar_wait_bounded(&wbar[cb ^ 1], (phase_bits >> (cb ^ 1)) & 1u, p.timeout_ns);
                         }
-                        __syncthreads();
+                        warp_failed = true;
                         break;
                     }
                     phase_bits ^= 1u << cb;
-                    const int* buf = tma_buf[cb];
+                    const int* buf = wbuf0 + cb * (P + 16);
                     const int tw = off + cnt;
-                    for (int base = 0; base < tw; base += 4 * B) {
-                        const int w4 = base + 4 * tid;
+                    for (int base = 0; base < tw; base += 128) {
+                        const int w4 = base + 4 * lane;
                         int4 x = make_int4(0, 0, 0, 0);
                         unsigned vm = 0;
                         if (w4 < tw) {
@@ -652,91 +711,87 @@ __global__ void __launch_bounds__(B) dfq_bfs_kernel(Params p) {
                                 if (w4 + j >= off && w4 + j < tw) vm |= 1u << j;
                         }
                         const int v[4] = {x.x, x.y, x.z, x.w};
-                        visit4(c, v, vm, par);
+                        visit4<PAR>(p, lv, t, v, vm, par);
                     }
                 } else {
-                    const int a0 = e0 - off, e1 = e0 + cnt;
-                    for (int base = a0; base < e1; base += 4 * B) {
-                        const int k4 = base + 4 * tid;
-                        int4 x = make_int4(0, 0, 0, 0);
-                        unsigned vm = 0;
-                        if (k4 < e1) {
-                            x = ldg4(p.cols + k4);
-#pragma unroll
-                            for (int j = 0; j < 4; ++j)
-                                if (k4 + j >= e0 && k4 + j < e1) vm |= 1u << j;
-                        }
-                        const int v[4] = {x.x, x.y, x.z, x.w};
-                        visit4(c, v, vm, par);
-                    }
+                    warp_expand<PAR>(p, lv, t, e0, cnt, par0);
                 }
-                __syncthreads();
+                __syncwarp();
                 cb ^= 1;
             }
-            __syncthreads();
         }
 
-        // (3) global overflow queue, dynamic chunks
+        // (3) global overflow queue in 32-entry chunks, same schedule as the
+        //     pieces; the next chunk index is fetched before the current one
+        //     is expanded
         if (n_ovf > 0) {
-            const int G4 = 4 * (int)gridDim.x;
-            int CH = (n_ovf + G4 - 1) / G4;
-            CH = CH < 32 ? 32 : (CH > B ? B : CH);
             const int2* ovf_in = p.ovf[in];
             const int* ovfv_in = p.ovfv[in];
+            const int n_chunks = (n_ovf + 31) >> 5;
+            const int c_static = n_chunks <= nwarps ? n_chunks : n_chunks - (n_chunks >> 2);
+            int s_next = gwarp;
+            auto next_chunk = [&]() -> int {  // lane 0 only
+                if (s_next < c_static) { const int ci = s_next; s_next += nwarps; return ci; }
+                if (c_static < n_chunks) return c_static + atomicAdd(&cin->ovf_grab, 1);
+                return n_chunks;
+            };
+            int nxt = 0;
+            if (lane == 0) nxt = next_chunk();
             while (true) {
-                if (tid == 0) s_bc = atomicAdd(&cin->ovf_grab, CH);
-                __syncthreads();
-                const int c0 = s_bc;
-                if (c0 >= n_ovf) break;
-                const int m = n_ovf - c0 < CH ? n_ovf - c0 : CH;
-                if (tid < m) {
-                    const int2 x = __ldcg(ovf_in + c0 + tid);
-                    st_start[tid] = x.x;
-                    st_deg[tid] = x.y;
-                    if (PAR) st_v[tid] = __ldcg(ovfv_in + c0 + tid);
+                const int ci = __shfl_sync(kFull, nxt, 0);
+                if (ci >= n_chunks) break;
+                const int c0 = ci << 5;
+                if (lane == 0) nxt = next_chunk();
+                const int i = c0 + lane;
+                const bool has = i < n_ovf;
+                int2 x = make_int2(0, 0);
+                int u = 0;
+                if (has) {
+                    x = __ldcg(ovf_in + i);
+                    if (PAR) u = __ldcg(ovfv_in + i);
                 }
-                __syncthreads();
-                process_entries<B, PAR>(c, st_start, st_deg, st_v, m, scan, mlist, s_warp, p.medium_min);
+                warp_process<PAR>(p, lv, t, wl, has, x.x, x.y, u);
             }
-            __syncthreads();
         }
 
         // end of level: publish how much this block pushed, keep its queue
         __syncthreads();
         if (tid == 0) {
-            const int kept = s_cnt_next < cap ? s_cnt_next : cap;
-            const int tot = kept + s_ovf_pushed + s_large_pushed;
-            if (tot) atomicAdd(&c.cout->pushed, tot);
-            if (s_claimed) atomicMax(&ctl->stats.depth, L + 1);
-            my_overflow += (unsigned long long)s_ovf_pushed;
-            my_large += (unsigned long long)s_large_pushed;
-            s_cnt_cur = kept;
-            s_cnt_next = 0;
-            s_ovf_pushed = s_large_pushed = s_claimed = 0;
+            const int kept = (int)(sh.local_pack >> 32);
+            const int tot = kept + sh.ovf_pushed + sh.large_pushed;
+            if (tot) atomicAdd(&ctl->lv[lv.cslot].pushed, tot);
+            if (sh.claimed) sh.depth = L + 1;
+            sh.overflow += (unsigned long long)sh.ovf_pushed;
+            sh.large += (unsigned long long)sh.large_pushed;
+            sh.cnt_cur = kept;
+            sh.local_pack = 0ull;
+            sh.local_grab = 0;
+            sh.ovf_pushed = sh.large_pushed = sh.claimed = 0;
         }
         cur ^= 1;
-        ok = grid_barrier(ctl, bar_target, p.timeout_ns, &s_flag);
+        ok = grid_barrier(ctl, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in);
     }
 
     // ---- statistics
-    unsigned long long e = c.edges, cl = c.claims;
+    unsigned long long e = t.edges, cl = t.claims;  // warp sums may pass 2^32
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         e += __shfl_down_sync(kFull, e, o);
         cl += __shfl_down_sync(kFull, cl, o);
     }
-    if (tid == 0) { s_red[0] = 0; s_red[1] = 0; }
+    if (tid == 0) { sh.red[0] = 0; sh.red[1] = 0; }
     __syncthreads();
-    if ((tid & 31) == 0) {
-        atomicAdd(&s_red[0], e);
-        atomicAdd(&s_red[1], cl);
+    if (lane == 0) {
+        atomicAdd(&sh.red[0], e);
+        atomicAdd(&sh.red[1], cl);
     }
     __syncthreads();
     if (tid == 0) {
-        atomicAdd(&ctl->stats.edges, s_red[0]);
-        atomicAdd(&ctl->stats.claims, s_red[1]);
-        atomicAdd(&ctl->stats.overflow, my_overflow);
-        atomicAdd(&ctl->stats.large, my_large);
+        atomicAdd(&ctl->stats.edges, sh.red[0]);
+        atomicAdd(&ctl->stats.claims, sh.red[1]);
+        atomicAdd(&ctl->stats.overflow, sh.overflow);
+        atomicAdd(&ctl->stats.large, sh.large);
+        if (sh.depth) atomicMax(&ctl->stats.depth, sh.depth);
         if (blockIdx.x == 0) ctl->stats.levels = L;
     }
 }

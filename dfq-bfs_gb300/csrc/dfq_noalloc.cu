@@ -139,7 +139,7 @@ extern "C" int dfq_bfs_noalloc(const int32_t* offsets, const int32_t* cols, int3
     const ScratchLayout sl = scratch_layout(n, e, o);
     if (sl.total > (size_t)DFQ_NOALLOC_SCRATCH_BYTES)
         return fail(DFQ_ENOMEM, "dfq_bfs_noalloc: a graph with n=%d, e=%lld needs %zu bytes of scratch; the fixed "
-                    "scratch array holds %zu (about 24 bytes per vertex); use dfq_graph_create for larger graphs",
+                    "scratch array holds %zu (24 bytes per vertex + 0.2 per edge); use dfq_graph_create for larger graphs",
                     n, (long long)e, sl.total, (size_t)DFQ_NOALLOC_SCRATCH_BYTES);
     int dev = 0;
     cudaError_t err = cudaGetDevice(&dev);
@@ -186,6 +186,7 @@ extern "C" int dfq_bfs_noalloc(const int32_t* offsets, const int32_t* cols, int3
     p.large_min = o.large_min_degree;
     p.piece_edges = o.piece_edges;
     p.local_cap = o.local_queue_cap;
+    p.local_budget = o.local_edge_budget;
     p.probe_first = o.probe_first;
     p.use_tma = o.use_tma;
     p.timeout_ns = (long long)o.timeout_ms * 1000000LL;

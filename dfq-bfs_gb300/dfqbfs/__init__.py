@@ -37,7 +37,7 @@ EXPORTS = [
     "dfq_opts_default", "dfq_graph_create", "dfq_graph_destroy", "dfq_graph_get_opts",
     "dfq_graph_set_opts", "dfq_graph_stream", "dfq_graph_num_vertices", "dfq_graph_num_edges",
     "dfq_bfs", "dfq_bfs_launch", "dfq_graph_sync", "dfq_bfs_last_stats", "dfq_autotune",
-    "dfq_bfs_noalloc",
+    "dfq_bfs_noalloc", "dfq_bfs_last_trace",
 ]
 
 
@@ -56,7 +56,8 @@ class _Csr(C.Structure):
 class Opts(C.Structure):
     _fields_ = [("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("medium_min_degree", C.c_int32), ("large_min_degree", C.c_int32),
-                ("local_queue_cap", C.c_int32), ("piece_edges", C.c_int32),
+                ("local_queue_cap", C.c_int32), ("local_edge_budget", C.c_int32),
+                ("piece_edges", C.c_int32),
                 ("probe_first", C.c_int32), ("l2_persist", C.c_int32),
                 ("use_tma", C.c_int32), ("timeout_ms", C.c_int32)]
 
@@ -117,6 +118,8 @@ def lib() -> C.CDLL:
     L.dfq_graph_sync.argtypes = [C.c_void_p]
     L.dfq_bfs_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     L.dfq_autotune.argtypes = [C.c_void_p, P32, C.c_int32, C.POINTER(Opts)]
+    L.dfq_bfs_last_trace.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32]
+    L.dfq_bfs_last_trace.restype = C.c_int
     L.dfq_bfs_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_int32, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.POINTER(Stats)]
     for name in ("dfq_csr_load", "dfq_csr_save", "dfq_csr_from_edges", "dfq_gen_zipf_geometric",
@@ -316,6 +319,15 @@ class Graph:
         st = Stats()
         check(lib().dfq_bfs_last_stats(self.h, C.byref(st)))
         return st
+
+    def last_trace(self, max_levels: int = 64):
+        """(start_ns[int64], frontier[int32]) of the first levels of the last launch."""
+        ns = np.zeros(max_levels, np.int64)
+        fr = np.zeros(max_levels, np.int32)
+        k = lib().dfq_bfs_last_trace(self.h, ns.ctypes.data_as(C.POINTER(C.c_int64)), _p32(fr), max_levels)
+        if k < 0:
+            check(k)
+        return ns[:k], fr[:k]
 
     def autotune(self, sources) -> Opts:
         s = np.ascontiguousarray(sources, dtype=np.int32)

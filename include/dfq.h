@@ -126,8 +126,13 @@ typedef struct dfq_opts {
                                    for the medium bin (one warp per vertex, int4 loads) */
     int32_t large_min_degree;   /* deg >= this goes to the grid-wide large bin */
     int32_t local_queue_cap;    /* per-block shared-memory frontier slots (0 = default) */
-    int32_t piece_edges;        /* large-bin piece size in edges (multiple of 64) */
-    int32_t probe_first;        /* 1: read the visited bitmap before the atomic claim */
+    int32_t local_edge_budget;  /* edges a block may keep in its shared-memory queue per
+                                   level; the rest overflows to the global queue (0 = default) */
+    int32_t piece_edges;        /* large-bin piece: edges one warp stages and expands
+                                   (multiple of 64) */
+    int32_t probe_first;        /* 1: read the visited bitmap before the atomic claim;
+                                   0: claim at once and fetch row bounds alongside;
+                                   2: choose per level by frontier size */
     int32_t l2_persist;         /* 1: visited bitmap in an L2 persisting access window */
     int32_t use_tma;            /* 1: stage large-bin pieces into smem with cp.async.bulk */
     int32_t timeout_ms;         /* bound on every device-side wait (0 = 5000) */
@@ -189,6 +194,14 @@ int dfq_graph_sync(dfq_graph* g);
 /* Counters of the last completed launch on this graph (kernel_ms = 0 here). */
 int dfq_bfs_last_stats(dfq_graph* g, dfq_stats* stats);
 
+/* Per-level trace of the last completed launch: for the first min(levels,
+ * max_levels, 64) levels, the device clock (ns) when the level started and the
+ * number of frontier entries it expanded.  Returns the number of levels
+ * written (>= 0) or a negative status.  Replaces the reference's per-level
+ * frontier profiler (design/shared-q/atomic-sa/our-sep/upper-bound/
+ * bfs_ftr_prof.cu:98-144, printed from the device at :206-208). */
+int dfq_bfs_last_trace(dfq_graph* g, int64_t* start_ns, int32_t* frontier, int32_t max_levels);
+
 /* Choose opts for this graph by timing candidate settings on a few sources;
  * writes the winner to *best and installs it on the graph. */
 int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, dfq_opts* best);
@@ -207,8 +220,8 @@ int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, dfq_opts* b
  * frontier queues, control block) is one fixed array of
  * DFQ_NOALLOC_SCRATCH_BYTES inside libdfq that every GPU loading the library
  * holds until the process exits.  That bounds the graph to roughly
- * n * 24 bytes plus (e/2048 + e/1024) * 20 bytes of scratch (about 1.3 million
- * vertices); larger graphs are rejected with DFQ_ENOMEM and a message naming
+ * 24 * n + e / 5 bytes of scratch (about 1.2 million vertices at average
+ * degree 16); larger graphs are rejected with DFQ_ENOMEM and a message naming
  * the bytes needed.  cols must be 16-byte aligned.  The CSR is checked on the
  * device first (DFQ_EFORMAT if malformed).
  *

@@ -105,15 +105,16 @@ def test_boundaries_all_block_sizes(boundary_graph, B, tma, probe):
     run_and_check(boundary_graph, 0, opts(block_threads=B, use_tma=tma, probe_first=probe))
 
 
-@pytest.mark.parametrize("medium,large,piece", [
-    (1, 32, 64),          # everything medium or large, tiny pieces
-    (1 << 30, 1 << 30, 2048),  # no medium, no large: all block-gathered
-    (8, 64, 128),
-    (32, 1024, 4096),
-    (64, 16384, 16384),
+@pytest.mark.parametrize("medium,large,piece,budget", [
+    (1, 32, 64, 8192),              # everything medium or large, tiny pieces
+    (1 << 30, 1 << 30, 256, 8192),  # no medium, no large: all warp-gathered
+    (8, 64, 128, 64),
+    (32, 1024, 512, 1 << 30),       # unlimited local edge budget
+    (64, 16384, 1024, 1),           # every warp batch overflows to the global queue
 ])
-def test_bin_thresholds(boundary_graph, medium, large, piece):
-    run_and_check(boundary_graph, 0, opts(medium_min_degree=medium, large_min_degree=large, piece_edges=piece))
+def test_bin_thresholds(boundary_graph, medium, large, piece, budget):
+    run_and_check(boundary_graph, 0, opts(medium_min_degree=medium, large_min_degree=large, piece_edges=piece,
+                                          local_edge_budget=budget))
 
 
 @pytest.mark.parametrize("cap", [1, 16, 100])
@@ -127,7 +128,7 @@ def test_forced_overflow(cap):
 def test_large_bin_used():
     g = d.gen_rmat(16, 16, seed=4)
     src = int(g.pick_sources(1, seed=4)[0])
-    _, st = run_and_check(g, src, opts(large_min_degree=256, piece_edges=256))
+    _, st = run_and_check(g, src, opts(large_min_degree=256, piece_edges=64))
     assert st.large > 0
 
 
