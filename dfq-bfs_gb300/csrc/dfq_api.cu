@@ -83,7 +83,7 @@ int validate_opts(const dfq_opts& o) {
     if (o.local_edge_budget < 0) return fail(DFQ_EINVAL, "local_edge_budget must be >= 0");
     if (o.timeout_ms < 1) return fail(DFQ_EINVAL, "timeout_ms must be >= 1");
     if (o.probe_first < 0 || o.probe_first > 2) return fail(DFQ_EINVAL, "probe_first must be 0, 1 or 2");
-    const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges);
+    const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true);
     if (L.bytes > 200 * 1024)
         return fail(DFQ_EINVAL, "options need %d bytes of shared memory per block (max 204800)", L.bytes);
     return DFQ_OK;
@@ -194,7 +194,7 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     const bool par = parents != nullptr;
     KernelFn k = pick_kernel(o.block_threads, par);
     if (!k) return fail(DFQ_EINVAL, "no kernel for block_threads=%d", o.block_threads);
-    const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges);
+    const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
     CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.bytes));
     int per_sm = 0;
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k, o.block_threads, lay.bytes));
@@ -275,7 +275,7 @@ void dfq_opts_default(dfq_opts* o) {
     o->blocks_per_sm = 0;
     o->medium_min_degree = 32;
     o->large_min_degree = 256;
-    o->local_queue_cap = 1024;
+    o->local_queue_cap = 256;
     o->local_edge_budget = 8192;
     o->piece_edges = 256;
     o->probe_first = 2;
@@ -295,7 +295,7 @@ int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int
     dfq_opts_default(&o);
     if (opts) o = *opts;
     if (o.block_threads == 0) o.block_threads = 512;
-    if (o.local_queue_cap == 0) o.local_queue_cap = 1024;
+    if (o.local_queue_cap == 0) o.local_queue_cap = 256;
     if (o.local_edge_budget == 0) o.local_edge_budget = 8192;
     if (o.timeout_ms == 0) o.timeout_ms = 5000;
     int rc = validate_opts(o);
@@ -392,7 +392,7 @@ int dfq_graph_set_opts(dfq_graph* g, const dfq_opts* o) {
     if (!g || !o) return fail(DFQ_EINVAL, "dfq_graph_set_opts: null argument");
     dfq_opts v = *o;
     if (v.block_threads == 0) v.block_threads = 512;
-    if (v.local_queue_cap == 0) v.local_queue_cap = 1024;
+    if (v.local_queue_cap == 0) v.local_queue_cap = 256;
     if (v.local_edge_budget == 0) v.local_edge_budget = 8192;
     if (v.timeout_ms == 0) v.timeout_ms = 5000;
     int rc = validate_opts(v);

@@ -229,19 +229,23 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
 }
 
 // ------------------------------------------------------------ shared layout
+constexpr int kRing = 256;  // per-warp candidate ring (entries, power of two)
+
 struct SmemLayout {
-    int q_off;    // local queues: 2 buffers x {start, deg, v} x cap ints
-    int wl_off;   // per-warp gather scratch: {scan, start, parent} x 32 ints
-    int tma_off;  // per-warp piece buffers: 2 x (piece + 16) ints, 128-byte aligned
-    int bar_off;  // per-warp mbarriers: 2 x u64
+    int q_off;     // local queues: 2 buffers x {start, deg, v} x cap ints
+    int wl_off;    // per-warp gather scratch: {scan, start, parent} x 32 ints
+    int ring_off;  // per-warp candidate ring: kRing vertices (+ kRing parents)
+    int tma_off;   // per-warp piece buffers: 2 x (piece + 16) ints, 128-byte aligned
+    int bar_off;   // per-warp mbarriers: 2 x u64
     int bytes;
 };
-__host__ __device__ inline SmemLayout smem_layout(int B, int cap, int piece) {
+__host__ __device__ inline SmemLayout smem_layout(int B, int cap, int piece, bool par) {
     SmemLayout L;
     const int NW = B / 32;
     int o = 0;
     L.q_off = o;    o += 2 * 3 * cap * 4;
     L.wl_off = o;   o += NW * 3 * 32 * 4;
+    L.ring_off = o; o += NW * kRing * (par ? 2 : 1) * 4;
     o = (o + 127) & ~127;
     L.tma_off = o;  o += NW * 2 * (piece + 16) * 4;
     o = (o + 15) & ~15;
@@ -287,6 +291,14 @@ struct Lv {
 struct Tally {
     unsigned edges;
     unsigned claims;
+};
+
+// This warp's ring of unvisited candidates (probe levels): entries
+// [head, head + n) modulo kRing; head and n are warp-uniform.
+struct Ring {
+    int* v;    // kRing vertices, then kRing parents when parents are kept
+    int head;
+    int n;
 };
 
 // Push up to four claimed vertices per lane into the block's next local
@@ -451,10 +463,105 @@ __device__ __forceinline__ void visit4(const Params& p, const Lv& lv, Tally& t, 
     push_local<PAR>(p, lv, loc, st, dg, v);
 }
 
+// Claim one candidate per lane (has == false: none) and record / push what
+// it wins.  Warp-collective.
+template <bool PAR>
+__device__ __forceinline__ void claim1(const Params& p, const Lv& lv, Tally& t, bool has, int v, int par) {
+    bool won = false;
+    if (has) {
+        const unsigned bit = 1u << (v & 31);
+        won = !(atomicOr(&p.bitmap[v >> 5], bit) & bit);
+    }
+    int st[4] = {0, 0, 0, 0}, dg[4] = {0, 0, 0, 0};
+    const int vv[4] = {v, 0, 0, 0};
+    unsigned loc = 0;
+    if (won) {
+        p.levels[v] = lv.next;
+        if (PAR) p.parents[v] = par;
+        st[0] = __ldg(p.offsets + v);
+        dg[0] = __ldg(p.offsets + v + 1) - st[0];
+        t.claims += 1;
+        sh.claimed = 1;
+        if (dg[0] >= p.large_min) push_large(p, lv, st[0], dg[0], v);
+        else if (dg[0] > 0) loc = 1;
+    }
+    push_local<PAR>(p, lv, loc, st, dg, vv);
+}
+
+// Claim buffered candidates 32 at a time while at least 32 are waiting (or
+// until the ring is empty when `all`).  Warp-collective.
+template <bool PAR>
+__device__ __forceinline__ void ring_drain(const Params& p, const Lv& lv, Tally& t, Ring& r, bool all) {
+    const int lane = threadIdx.x & 31;
+    while (r.n >= 32 || (all && r.n > 0)) {
+        const int take = r.n < 32 ? r.n : 32;
+        const bool has = lane < take;
+        int v = 0, par = 0;
+        if (has) {
+            const int idx = (r.head + lane) & (kRing - 1);
+            v = r.v[idx];
+            if (PAR) par = r.v[kRing + idx];
+        }
+        __syncwarp();
+        r.head = (r.head + take) & (kRing - 1);
+        r.n -= take;
+        claim1<PAR>(p, lv, t, has, v, par);
+    }
+}
+
+// Probe levels: test up to four neighbours per lane against the visited
+// bitmap and append the unvisited ones to the warp's ring (prefix-sum
+// compaction); claims happen in full-warp batches in ring_drain.  The ring
+// holds < 32 entries between calls, so one call (<= 128 appends) never wraps
+// onto unclaimed entries.  Warp-collective.
+template <bool PAR>
+__device__ __forceinline__ void probe4(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[4],
+                                       unsigned vmask, const int (&par)[4]) {
+    const int lane = threadIdx.x & 31;
+    unsigned w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) w[j] = (vmask >> j & 1) ? p.bitmap[v[j] >> 5] : 0xffffffffu;
+    unsigned cm = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if ((vmask >> j & 1) && !((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
+    t.edges += __popc(vmask);
+    const int c = __popc(cm);
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int tt = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += tt;
+    }
+    const int tot = __shfl_sync(kFull, incl, 31);
+    if (tot == 0) return;
+    int pos = r.head + r.n + incl - c;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (cm >> j & 1) {
+            const int idx = pos & (kRing - 1);
+            r.v[idx] = v[j];
+            if (PAR) r.v[kRing + idx] = par[j];
+            ++pos;
+        }
+    }
+    __syncwarp();
+    r.n += tot;
+    ring_drain<PAR>(p, lv, t, r, false);
+}
+
+// Probe or claim-at-once, by level.  Warp-collective.
+template <bool PAR>
+__device__ __forceinline__ void scan4(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[4],
+                                      unsigned vmask, const int (&par)[4]) {
+    if (lv.probe) probe4<PAR>(p, lv, t, r, v, vmask, par);
+    else visit4<PAR>(p, lv, t, v, vmask, par);
+}
+
 // One warp expands one list [s, s+d): int4 column loads from the 16-byte
 // aligned floor of the list; lanes mask what lies outside it.
 template <bool PAR>
-__device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally& t, int s, int d, int u) {
+__device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally& t, Ring& r, int s, int d, int u) {
     const int lane = threadIdx.x & 31;
     const int e0 = s, e1 = s + d;
     const int par[4] = {u, u, u, u};
@@ -469,7 +576,7 @@ __device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally
                 if (k4 + j >= e0 && k4 + j < e1) vm |= 1u << j;
         }
         const int v[4] = {x.x, x.y, x.z, x.w};
-        visit4<PAR>(p, lv, t, v, vm, par);
+        scan4<PAR>(p, lv, t, r, v, vm, par);
     }
 }
 
@@ -478,8 +585,8 @@ __device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally
 // gather over the concatenation of their lists (4 edges per lane per round).
 // wl: this warp's 96-int scratch (scan, start, parent).  Warp-collective.
 template <bool PAR>
-__device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tally& t, int* wl, bool has, int s,
-                                             int d, int u) {
+__device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tally& t, Ring& r, int* wl, bool has,
+                                             int s, int d, int u) {
     const int lane = threadIdx.x & 31;
     if (!has) d = 0;
     const bool med = d >= p.medium_min;
@@ -487,7 +594,7 @@ __device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tall
     while (mmask) {
         const int i = __ffs(mmask) - 1;
         mmask &= mmask - 1;
-        warp_expand<PAR>(p, lv, t, __shfl_sync(kFull, s, i), __shfl_sync(kFull, d, i), __shfl_sync(kFull, u, i));
+        warp_expand<PAR>(p, lv, t, r, __shfl_sync(kFull, s, i), __shfl_sync(kFull, d, i), __shfl_sync(kFull, u, i));
     }
     const int ds = med ? 0 : d;
     int incl = ds;
@@ -524,7 +631,7 @@ __device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tall
                 vm |= 1u << j;
             }
         }
-        visit4<PAR>(p, lv, t, v, vm, par);
+        scan4<PAR>(p, lv, t, r, v, vm, par);
     }
 }
 
@@ -535,9 +642,13 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
     // grid-wide warp index, interleaved across blocks so that consecutive
     // statically assigned chunks land on different SMs
     const int gwarp = warp * (int)gridDim.x + (int)blockIdx.x, nwarps = (int)gridDim.x * NW;
-    const SmemLayout lay = smem_layout(B, p.local_cap, p.piece_edges);
+    const SmemLayout lay = smem_layout(B, p.local_cap, p.piece_edges, PAR);
     const int P = p.piece_edges;
     int* wl = reinterpret_cast<int*>(dfq_smem + lay.wl_off) + warp * 96;
+    Ring ring;
+    ring.v = reinterpret_cast<int*>(dfq_smem + lay.ring_off) + warp * kRing * (PAR ? 2 : 1);
+    ring.head = 0;
+    ring.n = 0;
     int* wbuf0 = reinterpret_cast<int*>(dfq_smem + lay.tma_off) + warp * 2 * (P + 16);
     unsigned long long* wbar = reinterpret_cast<unsigned long long*>(dfq_smem + lay.bar_off) + warp * 2;
     Control* ctl = p.ctl;
@@ -635,7 +746,7 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
                 if (j >= nloc) break;
                 const int i = j + lane;
                 const bool has = i < nloc;
-                warp_process<PAR>(p, lv, t, wl, has, has ? qc[i] : 0, has ? qc[p.local_cap + i] : 0,
+                warp_process<PAR>(p, lv, t, ring, wl, has, has ? qc[i] : 0, has ? qc[p.local_cap + i] : 0,
                                   (PAR && has) ? qc[2 * p.local_cap + i] : 0);
             }
         }
@@ -711,10 +822,10 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
                                 if (w4 + j >= off && w4 + j < tw) vm |= 1u << j;
                         }
                         const int v[4] = {x.x, x.y, x.z, x.w};
-                        visit4<PAR>(p, lv, t, v, vm, par);
+                        scan4<PAR>(p, lv, t, ring, v, vm, par);
                     }
                 } else {
-                    warp_expand<PAR>(p, lv, t, e0, cnt, par0);
+                    warp_expand<PAR>(p, lv, t, ring, e0, cnt, par0);
                 }
                 __syncwarp();
                 cb ^= 1;
@@ -750,9 +861,11 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
                     x = __ldcg(ovf_in + i);
                     if (PAR) u = __ldcg(ovfv_in + i);
                 }
-                warp_process<PAR>(p, lv, t, wl, has, x.x, x.y, u);
+                warp_process<PAR>(p, lv, t, ring, wl, has, x.x, x.y, u);
             }
         }
+        // claim whatever candidates this warp still holds
+        ring_drain<PAR>(p, lv, t, ring, true);
 
         // end of level: publish how much this block pushed, keep its queue
         __syncthreads();

@@ -47,7 +47,7 @@ struct DeviceSetup {
     unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
     int sms = 0;
     int grid[2] = {0, 0};  // without / with parents
-    int smem = 0;
+    int smem[2] = {0, 0};  // without / with parents
 };
 
 std::mutex g_setup_mu;
@@ -103,10 +103,11 @@ int setup_device(int dev, const dfq_opts& o, DeviceSetup** out) {
         err = cudaGetDeviceProperties(&prop, dev);
         if (err != cudaSuccess) return fail(DFQ_ECUDA, "dfq_bfs_noalloc: %s", cudaGetErrorString(err));
         if (!prop.cooperativeLaunch) return fail(DFQ_ECUDA, "dfq_bfs_noalloc: no cooperative launch on device %d", dev);
-        const dfqk::SmemLayout lay = dfqk::smem_layout(kBlock, o.local_queue_cap, o.piece_edges);
         const void* fns[2] = {(const void*)dfqk::dfq_bfs_kernel<kBlock, false>,
                               (const void*)dfqk::dfq_bfs_kernel<kBlock, true>};
         for (int i = 0; i < 2; ++i) {
+            const dfqk::SmemLayout lay = dfqk::smem_layout(kBlock, o.local_queue_cap, o.piece_edges, i == 1);
+            d.smem[i] = lay.bytes;
             err = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, lay.bytes);
             int per_sm = 0;
             if (err == cudaSuccess)
@@ -116,7 +117,6 @@ int setup_device(int dev, const dfq_opts& o, DeviceSetup** out) {
             d.grid[i] = prop.multiProcessorCount * per_sm;
         }
         d.sms = prop.multiProcessorCount;
-        d.smem = lay.bytes;
         d.scratch = (unsigned char*)addr;
         d.ready = true;
     }
@@ -194,7 +194,7 @@ extern "C" int dfq_bfs_noalloc(const int32_t* offsets, const int32_t* cols, int3
     const void* fn = par ? (const void*)dfqk::dfq_bfs_kernel<kBlock, true> : (const void*)dfqk::dfq_bfs_kernel<kBlock, false>;
     void* args[] = {&p};
     if ((err = cudaMemsetAsync(ctl, 0, sizeof(dfqk::Control), s)) != cudaSuccess ||
-        (err = cudaLaunchCooperativeKernel(fn, dim3(ds->grid[par ? 1 : 0]), dim3(kBlock), args, ds->smem, s)) !=
+        (err = cudaLaunchCooperativeKernel(fn, dim3(ds->grid[par ? 1 : 0]), dim3(kBlock), args, ds->smem[par ? 1 : 0], s)) !=
             cudaSuccess ||
         (err = cudaMemcpyAsync(&host_ctl, ctl, sizeof(host_ctl), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (err = cudaStreamSynchronize(s)) != cudaSuccess)
