@@ -55,7 +55,8 @@ struct alignas(128) LevelCtr {
     int ovf_count;                  // entries in the global overflow queue
     int pushed;                     // frontier entries (local + overflow + large)
     unsigned long long large_pack;  // (large entries << 32) | pieces
-    int pad0[28];
+    int pushed_edges;               // sum of the degrees of those entries
+    int pad0[27];
     int ovf_grab;                   // chunk cursor over the overflow queue
     int pad1[31];
     int large_grab;                 // piece cursor over the large queue
@@ -130,6 +131,26 @@ __device__ __forceinline__ void prefetch_l2(const void* p) {
     asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 __device__ __forceinline__ int4 ldg4(const int* p) { return __ldg(reinterpret_cast<const int4*>(p)); }
+// L2 policy for the column stream: each column is read once per BFS, so its
+// lines are the first to go and the randomly read row bounds, level array and
+// visited bitmap keep their L2 residency; L1 is left to the bitmap.
+__device__ __forceinline__ unsigned long long policy_stream() {
+    unsigned long long pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ int4 ldg4_stream(const int* ptr) {
+    int4 v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(ptr), "l"(policy_stream()));
+    return v;
+}
+__device__ __forceinline__ int ldg_stream(const int* ptr) {
+    int v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(ptr), "l"(policy_stream()));
+    return v;
+}
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
     return (unsigned)__cvta_generic_to_shared(p);
 }
@@ -158,10 +179,12 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
 // dst, src 16-byte aligned; bytes a multiple of 16.
 __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes,
                                             unsigned long long* bar) {
+    unsigned long long pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
     asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+        "%4;" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
         : "memory");
 }
 
@@ -222,6 +245,7 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
             const unsigned long long lp = __ldcg(&next->large_pack);
             s_in[2] = (int)(lp >> 32);
             s_in[3] = (int)(unsigned)lp;
+            s_in[4] = __ldcg(&next->pushed_edges);
         }
     }
     __syncthreads();
@@ -268,7 +292,9 @@ struct BlockShared {
     int large_pushed;               // entries this block sent to the large queue
     int claimed;                    // this block claimed a vertex at this level
     int flag;                       // barrier verdict
-    int in[4];                      // this level's input: pushed, overflow, large entries, pieces
+    int in[5];                      // this level's input: pushed, overflow, large entries, pieces, edges
+    int ovf_edges;                  // degree sum of this block's overflow pushes at this level
+    int large_edges;                // degree sum of this block's large pushes at this level
     int depth;                      // deepest level this block claimed into
     unsigned long long overflow;    // entries this block sent to the overflow queue (whole BFS)
     unsigned long long large;       // entries this block sent to the large queue (whole BFS)
@@ -339,6 +365,7 @@ __device__ __forceinline__ void push_local(const Params& p, const Lv& lv, unsign
         if (base < 0) {
             gbase = atomicAdd(&p.ctl->lv[lv.cslot].ovf_count, tot);
             atomicAdd(&sh.ovf_pushed, tot);
+            atomicAdd(&sh.ovf_edges, dsum);
         }
     }
     base = __shfl_sync(kFull, base, 0);
@@ -380,6 +407,7 @@ __device__ __forceinline__ void push_large(const Params& p, const Lv& lv, int st
     const int slot = (int)(old >> 32);
     const unsigned poff = (unsigned)old;
     atomicAdd(&sh.large_pushed, 1);
+    atomicAdd(&sh.large_edges, dg);
     if (slot >= p.large_cap || poff + np > (unsigned)p.piece_cap) {
         set_error(p.ctl, kErrQueueCap, slot, (int)poff);
         return;
@@ -570,7 +598,7 @@ __device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally
         int4 x = make_int4(0, 0, 0, 0);
         unsigned vm = 0;
         if (k4 < e1) {
-            x = ldg4(p.cols + k4);
+            x = lv.probe ? ldg4_stream(p.cols + k4) : ldg4(p.cols + k4);
 #pragma unroll
             for (int j = 0; j < 4; ++j)
                 if (k4 + j >= e0 && k4 + j < e1) vm |= 1u << j;
@@ -626,7 +654,8 @@ __device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tall
 #pragma unroll
                 for (int step = 16; step > 0; step >>= 1)
                     if (wl[own + step] <= k) own += step;
-                v[j] = __ldg(p.cols + wl[32 + own] + (k - wl[own]));
+                const int* cp = p.cols + wl[32 + own] + (k - wl[own]);
+                v[j] = lv.probe ? ldg_stream(cp) : __ldg(cp);
                 if (PAR) par[j] = wl[64 + own];
                 vm |= 1u << j;
             }
@@ -678,12 +707,14 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
                     ctl->lv[0].ovf_count = 1;
                 }
                 ctl->lv[0].pushed = 1;
+                ctl->lv[0].pushed_edges = d;
             }
         }
     }
     if (tid == 0) {
         sh.local_pack = 0ull;
         sh.cnt_cur = sh.local_grab = sh.ovf_pushed = sh.large_pushed = sh.claimed = 0;
+        sh.ovf_edges = sh.large_edges = 0;
         sh.depth = 0;
         sh.overflow = sh.large = 0ull;
     }
@@ -715,6 +746,7 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
             cz->ovf_grab = 0;
             cz->large_grab = 0;
             cz->pushed = 0;
+            cz->pushed_edges = 0;
             cz->large_pack = 0ull;
         }
         const int in = L & 1;
@@ -731,9 +763,11 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
             const int share = (pushed + (int)gridDim.x - 1) / (int)gridDim.x;
             lv.cap = min(p.local_cap, max(32, 2 * share));
         }
-        // probe the bitmap before claiming only where many edges hit visited
-        // vertices (large frontiers); 2 = decide per level
-        lv.probe = p.probe_first == 2 ? (pushed >= 8 * nwarps ? 1 : 0) : p.probe_first;
+        // probe-then-claim where the level scans many edges (most of them hit
+        // visited vertices); claim at once, with row bounds fetched alongside,
+        // where it scans fewer edges than one 4-edge round per lane of the
+        // grid; 2 = decide per level
+        lv.probe = p.probe_first == 2 ? (sh.in[4] >= 128 * nwarps ? 1 : 0) : p.probe_first;
 
         // (1) this block's own queue from the previous level, 32 entries per grab
         {
@@ -872,7 +906,11 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
         if (tid == 0) {
             const int kept = (int)(sh.local_pack >> 32);
             const int tot = kept + sh.ovf_pushed + sh.large_pushed;
-            if (tot) atomicAdd(&ctl->lv[lv.cslot].pushed, tot);
+            if (tot) {
+                atomicAdd(&ctl->lv[lv.cslot].pushed, tot);
+                atomicAdd(&ctl->lv[lv.cslot].pushed_edges,
+                          (int)(unsigned)sh.local_pack + sh.ovf_edges + sh.large_edges);
+            }
             if (sh.claimed) sh.depth = L + 1;
             sh.overflow += (unsigned long long)sh.ovf_pushed;
             sh.large += (unsigned long long)sh.large_pushed;
@@ -880,6 +918,7 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
             sh.local_pack = 0ull;
             sh.local_grab = 0;
             sh.ovf_pushed = sh.large_pushed = sh.claimed = 0;
+            sh.ovf_edges = sh.large_edges = 0;
         }
         cur ^= 1;
         ok = grid_barrier(ctl, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in);
