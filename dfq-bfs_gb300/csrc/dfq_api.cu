@@ -282,6 +282,8 @@ void dfq_opts_default(dfq_opts* o) {
     o->l2_persist = 0;
     o->use_tma = 1;
     o->timeout_ms = 5000;
+    o->wide_min_edges = 1 << 21;
+    o->wide_min_degree = 8;
 }
 
 int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int64_t e, const dfq_opts* opts,

@@ -1,0 +1,693 @@
+// Graph pools and batched BFS: many graphs resident on the device, many
+// (graph, source) queries in one persistent cooperative launch.
+//
+// No reference counterpart: a reference program handles one graph and runs
+// one source per launch (design/shared-q/atomic-sa/our-sep/upper-bound/
+// bfs.cu:202-309).  The batch kernel reuses the single-source BFS body
+// (bfs_run) with two group shapes:
+//   wide queries   - graphs with many edges and a short diameter - run one
+//                    after another on the whole grid (grid barrier per level);
+//   narrow queries - small or high-diameter graphs - are pulled by blocks, and
+//                    each block runs its query alone, its block barrier being
+//                    the level barrier.  A level then costs a __syncthreads
+//                    instead of a grid barrier, and 2 x SMs queries proceed at
+//                    once.
+// Narrow queries are handed out largest-estimated-cost first.
+#include "common.hpp"
+#include "dfq_kernel.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+using namespace dfq;
+
+namespace dfqk {
+
+struct PoolGraph {
+    const int* offsets;
+    const int* cols;
+    int n;
+    int wide;
+    long long e;
+};
+
+// One query as the device sees it; start/end written by the kernel.
+struct BatchQuery {
+    int graph;
+    int source;
+    int* levels;
+    int* parents;
+    long long t_start;
+    long long t_end;
+};
+
+// BFS workspace: queues, bitmap and capacities for graphs up to n vertices.
+struct Workspace {
+    unsigned* bitmap;
+    int2* ovf[2];
+    int* ovfv[2];
+    int4* large[2];
+    int* piece_owner[2];
+    int large_cap;
+    int piece_cap;
+};
+
+// Byte layout of one workspace for graphs up to n vertices and e edges.
+struct WsLayout {
+    size_t bitmap, ovf[2], ovfv[2], large[2], owner[2], total;
+    int large_cap, piece_cap;
+};
+
+struct BatchParams {
+    const PoolGraph* graphs;
+    BatchQuery* queries;
+    Control* ctls;          // one per query, zeroed before the launch
+    const int* wide_list;   // query indices run on the whole grid, in order
+    int n_wide;
+    const int* narrow_list; // query indices run by one block, costliest first
+    int n_narrow;
+    int* narrow_next;       // cursor over narrow_list
+    long long* t0;          // device clock at the start of the launch
+    Workspace wide_ws;
+    unsigned char* block_ws;  // per-block workspaces, block_ws_stride bytes apart
+    size_t block_ws_stride;
+    WsLayout block_lay;       // layout of each of them
+    int medium_min, large_min, piece_edges, local_cap, local_budget, probe_first, use_tma;
+    long long timeout_ns;
+};
+
+inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+inline WsLayout ws_layout(long long n, long long e, int min_large, int min_piece, bool par) {
+    WsLayout w;
+    size_t o = 0;
+    w.bitmap = o;  o = al256(o + 4 * (size_t)(((n + 31) / 32 + 31) & ~31LL));
+    w.large_cap = (int)std::min<long long>(n, e / min_large + 1) + 1;
+    w.piece_cap = (int)std::min<long long>(1LL << 30, e / min_piece + w.large_cap + 2);
+    for (int i = 0; i < 2; ++i) { w.ovf[i] = o;   o = al256(o + 8 * (size_t)std::max<long long>(n, 1)); }
+    for (int i = 0; i < 2; ++i) { w.ovfv[i] = o;  o = al256(o + (par ? 4 * (size_t)std::max<long long>(n, 1) : 256)); }
+    for (int i = 0; i < 2; ++i) { w.large[i] = o; o = al256(o + 16 * (size_t)w.large_cap); }
+    for (int i = 0; i < 2; ++i) { w.owner[i] = o; o = al256(o + 4 * (size_t)w.piece_cap); }
+    w.total = o;
+    return w;
+}
+
+__device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, int qi, const Workspace& ws) {
+    const BatchQuery& q = bp.queries[qi];
+    const PoolGraph& g = bp.graphs[q.graph];
+    sp.offsets = g.offsets;
+    sp.cols = g.cols;
+    sp.n = g.n;
+    sp.src = q.source;
+    sp.levels = q.levels;
+    sp.parents = q.parents;
+    sp.bitmap = ws.bitmap;
+    sp.bitmap_words = (g.n + 31) / 32;
+    for (int i = 0; i < 2; ++i) {
+        sp.ovf[i] = ws.ovf[i];
+        sp.ovfv[i] = ws.ovfv[i];
+        sp.large[i] = ws.large[i];
+        sp.piece_owner[i] = ws.piece_owner[i];
+    }
+    sp.large_cap = ws.large_cap;
+    sp.piece_cap = ws.piece_cap;
+    sp.ctl = bp.ctls + qi;
+    sp.medium_min = bp.medium_min;
+    sp.large_min = bp.large_min;
+    sp.piece_edges = bp.piece_edges;
+    sp.local_cap = bp.local_cap;
+    sp.local_budget = bp.local_budget;
+    sp.probe_first = bp.probe_first;
+    sp.use_tma = bp.use_tma;
+    sp.timeout_ns = bp.timeout_ns;
+}
+
+template <int B, bool PAR>
+__global__ void __launch_bounds__(B, 1024 / B) dfq_batch_kernel(const __grid_constant__ BatchParams bp) {
+    __shared__ Params sp;
+    __shared__ int s_q;
+    init_warp_barriers<B, PAR>(bp.local_cap, bp.piece_edges);
+    WarpState ws{0u, false};
+    if (blockIdx.x == 0 && threadIdx.x == 0) *bp.t0 = (long long)globaltimer();
+
+    // wide queries: the whole grid, one after another
+    for (int k = 0; k < bp.n_wide; ++k) {
+        const int qi = bp.wide_list[k];
+        if (threadIdx.x == 0) {
+            fill_params(sp, bp, qi, bp.wide_ws);
+            if (blockIdx.x == 0) bp.queries[qi].t_start = (long long)globaltimer();
+        }
+        __syncthreads();
+        bfs_run<B, PAR>(sp, (int)gridDim.x, (int)blockIdx.x, ws);
+        if (blockIdx.x == 0 && threadIdx.x == 0) bp.queries[qi].t_end = (long long)globaltimer();
+        __syncthreads();
+    }
+
+    // narrow queries: each block pulls one at a time and runs it alone
+    Workspace bw;
+    {
+        unsigned char* base = bp.block_ws + bp.block_ws_stride * blockIdx.x;
+        const WsLayout& l = bp.block_lay;
+        bw.bitmap = (unsigned*)(base + l.bitmap);
+        for (int i = 0; i < 2; ++i) {
+            bw.ovf[i] = (int2*)(base + l.ovf[i]);
+            bw.ovfv[i] = (int*)(base + l.ovfv[i]);
+            bw.large[i] = (int4*)(base + l.large[i]);
+            bw.piece_owner[i] = (int*)(base + l.owner[i]);
+        }
+        bw.large_cap = l.large_cap;
+        bw.piece_cap = l.piece_cap;
+    }
+    while (true) {
+        if (threadIdx.x == 0) {
+            const int k = atomicAdd(bp.narrow_next, 1);
+            s_q = k < bp.n_narrow ? bp.narrow_list[k] : -1;
+            if (s_q >= 0) {
+                fill_params(sp, bp, s_q, bw);
+                bp.queries[s_q].t_start = (long long)globaltimer();
+            }
+        }
+        __syncthreads();
+        const int qi = s_q;
+        if (qi < 0) break;
+        bfs_run<B, PAR>(sp, 1, 0, ws);
+        if (threadIdx.x == 0) bp.queries[qi].t_end = (long long)globaltimer();
+        __syncthreads();
+    }
+}
+
+}  // namespace dfqk
+
+using namespace dfqk;
+
+struct dfq_pool {
+    int device = 0;
+    int sms = 0;
+    dfq_opts opts{};
+    int32_t ngraphs = 0;
+    std::vector<int32_t> n;
+    std::vector<int64_t> e;
+    std::vector<int32_t> wide;
+    std::vector<double> cost;
+    int32_t* offsets = nullptr;  // packed
+    int32_t* cols = nullptr;     // packed, each graph 16-byte aligned and padded
+    PoolGraph* d_graphs = nullptr;
+    std::vector<PoolGraph> h_graphs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // whole-grid workspace (largest graph) and per-block workspaces (largest narrow graph)
+    unsigned char* wide_mem = nullptr;
+    WsLayout wide_lay{};
+    bool wide_par = false;
+    unsigned char* block_mem = nullptr;
+    size_t block_stride = 0;
+    WsLayout block_lay{};
+    int block_grid = 0;
+    int block_n = 0;
+    bool block_par = false;
+    // batch tables
+    BatchQuery* d_queries = nullptr;
+    BatchQuery* h_queries = nullptr;  // pinned
+    int* d_lists = nullptr;
+    int* h_lists = nullptr;           // pinned: wide list then narrow list
+    Control* d_ctls = nullptr;
+    Control* h_ctls = nullptr;        // pinned
+    int* d_misc = nullptr;            // narrow cursor
+    long long* d_t0 = nullptr;
+    long long* h_t0 = nullptr;
+    int qcap = 0;
+    // captured batch
+    cudaGraphExec_t gexec = nullptr;
+    int g_nq = -1, g_nwide = -1, g_par = -1;
+    // single-query launches
+    Control* d_ctl1 = nullptr;
+    Control* h_ctl1 = nullptr;
+};
+
+namespace {
+
+constexpr int kMinLarge = 32, kMinPiece = 64, kColsPad = 32;
+
+template <class T>
+int dmalloc(T** p, size_t bytes) {
+    *p = nullptr;
+    cudaError_t err = cudaMalloc((void**)p, bytes ? bytes : 16);
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(err == cudaErrorMemoryAllocation ? DFQ_ENOMEM : DFQ_ECUDA, "cudaMalloc(%zu): %s", bytes,
+                    cudaGetErrorString(err));
+    }
+    return DFQ_OK;
+}
+
+void pool_release(dfq_pool* p) {
+    if (!p) return;
+    cudaSetDevice(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    cudaFree(p->offsets);
+    cudaFree(p->cols);
+    cudaFree(p->d_graphs);
+    cudaFree(p->wide_mem);
+    cudaFree(p->block_mem);
+    cudaFree(p->d_queries);
+    cudaFree(p->d_lists);
+    cudaFree(p->d_ctls);
+    cudaFree(p->d_misc);
+    cudaFree(p->d_t0);
+    cudaFree(p->d_ctl1);
+    if (p->h_queries) cudaFreeHost(p->h_queries);
+    if (p->h_lists) cudaFreeHost(p->h_lists);
+    if (p->h_ctls) cudaFreeHost(p->h_ctls);
+    if (p->h_t0) cudaFreeHost(p->h_t0);
+    if (p->h_ctl1) cudaFreeHost(p->h_ctl1);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+Workspace ws_from(unsigned char* base, const WsLayout& l) {
+    Workspace w;
+    w.bitmap = (unsigned*)(base + l.bitmap);
+    for (int i = 0; i < 2; ++i) {
+        w.ovf[i] = (int2*)(base + l.ovf[i]);
+        w.ovfv[i] = (int*)(base + l.ovfv[i]);
+        w.large[i] = (int4*)(base + l.large[i]);
+        w.piece_owner[i] = (int*)(base + l.owner[i]);
+    }
+    w.large_cap = l.large_cap;
+    w.piece_cap = l.piece_cap;
+    return w;
+}
+
+// (Re)allocate the whole-grid workspace for the largest graph, with parent
+// ids if asked.
+int ensure_wide(dfq_pool* p, bool par) {
+    if (p->wide_mem && (p->wide_par || !par)) return DFQ_OK;
+    cudaFree(p->wide_mem);
+    p->wide_mem = nullptr;
+    long long nmax = 1, emax = 0;
+    for (int i = 0; i < p->ngraphs; ++i) { nmax = std::max<long long>(nmax, p->n[i]); emax = std::max<long long>(emax, p->e[i]); }
+    p->wide_lay = ws_layout(nmax, emax, kMinLarge, kMinPiece, par);
+    p->wide_par = par;
+    return dmalloc(&p->wide_mem, p->wide_lay.total);
+}
+
+int grid_for(dfq_pool* p, const void* fn, int B, int smem, int* grid) {
+    cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int per_sm = 0;
+    if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B, smem);
+    if (err != cudaSuccess || per_sm < 1)
+        return fail(DFQ_ECUDA, "kernel does not fit: %s", cudaGetErrorString(err));
+    if (p->opts.blocks_per_sm > 0) per_sm = std::min(per_sm, p->opts.blocks_per_sm);
+    *grid = p->sms * per_sm;
+    return DFQ_OK;
+}
+
+// (Re)allocate the per-block workspaces for the largest narrow graph.
+int ensure_blocks(dfq_pool* p, int grid, bool par) {
+    long long nmax = 1, emax = 0;
+    for (int i = 0; i < p->ngraphs; ++i)
+        if (!p->wide[i]) { nmax = std::max<long long>(nmax, p->n[i]); emax = std::max<long long>(emax, p->e[i]); }
+    if (p->block_mem && p->block_grid >= grid && (p->block_par || !par) && p->block_n >= nmax) return DFQ_OK;
+    cudaFree(p->block_mem);
+    p->block_mem = nullptr;
+    p->block_lay = ws_layout(nmax, emax, kMinLarge, kMinPiece, par);
+    p->block_stride = al256(p->block_lay.total);
+    p->block_grid = grid;
+    p->block_n = (int)nmax;
+    p->block_par = par;
+    return dmalloc(&p->block_mem, p->block_stride * (size_t)grid);
+}
+
+int ensure_tables(dfq_pool* p, int nq) {
+    if (p->qcap >= nq) return DFQ_OK;
+    cudaFree(p->d_queries); cudaFree(p->d_lists); cudaFree(p->d_ctls);
+    if (p->h_queries) cudaFreeHost(p->h_queries);
+    if (p->h_lists) cudaFreeHost(p->h_lists);
+    if (p->h_ctls) cudaFreeHost(p->h_ctls);
+    p->d_queries = nullptr; p->d_lists = nullptr; p->d_ctls = nullptr;
+    p->h_queries = nullptr; p->h_lists = nullptr; p->h_ctls = nullptr;
+    p->qcap = 0;
+    int rc;
+    if ((rc = dmalloc(&p->d_queries, sizeof(BatchQuery) * nq))) return rc;
+    if ((rc = dmalloc(&p->d_lists, sizeof(int) * 2 * nq))) return rc;
+    if ((rc = dmalloc(&p->d_ctls, sizeof(Control) * nq))) return rc;
+    if (cudaMallocHost((void**)&p->h_queries, sizeof(BatchQuery) * nq) != cudaSuccess ||
+        cudaMallocHost((void**)&p->h_lists, sizeof(int) * 2 * nq) != cudaSuccess ||
+        cudaMallocHost((void**)&p->h_ctls, sizeof(Control) * nq) != cudaSuccess)
+        return fail(DFQ_ENOMEM, "pinned host tables for %d queries", nq);
+    p->qcap = nq;
+    if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; p->g_nq = -1; }
+    return DFQ_OK;
+}
+
+template <int B, bool PAR>
+void* batch_fn() { return (void*)dfq_batch_kernel<B, PAR>; }
+
+void* pick_batch(int B, bool par) {
+    switch (B) {
+        case 256: return par ? batch_fn<256, true>() : batch_fn<256, false>();
+        case 512: return par ? batch_fn<512, true>() : batch_fn<512, false>();
+        case 1024: return par ? batch_fn<1024, true>() : batch_fn<1024, false>();
+        default: return nullptr;
+    }
+}
+void* pick_single(int B, bool par) {
+    switch (B) {
+        case 256: return par ? (void*)dfq_bfs_kernel<256, true> : (void*)dfq_bfs_kernel<256, false>;
+        case 512: return par ? (void*)dfq_bfs_kernel<512, true> : (void*)dfq_bfs_kernel<512, false>;
+        case 1024: return par ? (void*)dfq_bfs_kernel<1024, true> : (void*)dfq_bfs_kernel<1024, false>;
+        default: return nullptr;
+    }
+}
+
+int launch_coop(const void* fn, int grid, int B, int smem, void* arg, cudaStream_t s) {
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(B);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {arg};
+    cudaError_t err = cudaLaunchKernelExC(&cfg, fn, args);
+    if (err != cudaSuccess) return fail(DFQ_ECUDA, "cooperative launch: %s", cudaGetErrorString(err));
+    return DFQ_OK;
+}
+
+int map_status(int st) {
+    switch (st) {
+        case kErrNone: return DFQ_OK;
+        case kErrBarrierTimeout:
+        case kErrTmaTimeout: return DFQ_ETIMEOUT;
+        default: return DFQ_EDEVICE;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int dfq_pool_create(const dfq_csr* graphs, int32_t ngraphs, const dfq_opts* opts, dfq_pool** out) {
+    clear_error();
+    if (!out || !graphs || ngraphs < 1) return fail(DFQ_EINVAL, "dfq_pool_create: need graphs");
+    *out = nullptr;
+    dfq_opts o;
+    dfq_opts_default(&o);
+    if (opts) o = *opts;
+    if (o.wide_min_edges <= 0) o.wide_min_edges = 1 << 21;
+    if (o.wide_min_degree <= 0) o.wide_min_degree = 8;
+    if (o.block_threads == 0) o.block_threads = 512;
+    if (o.local_queue_cap == 0) o.local_queue_cap = 256;
+    if (o.local_edge_budget == 0) o.local_edge_budget = 8192;
+    if (o.timeout_ms == 0) o.timeout_ms = 5000;
+    dfq_pool* p = new dfq_pool();
+    p->opts = o;
+    p->ngraphs = ngraphs;
+    cudaGetDevice(&p->device);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, p->device) != cudaSuccess) { pool_release(p); return fail(DFQ_ECUDA, "no CUDA device"); }
+    p->sms = prop.multiProcessorCount;
+    int64_t tot_n = 0, tot_e = 0;
+    std::vector<int64_t> off_base(ngraphs), col_base(ngraphs);
+    for (int i = 0; i < ngraphs; ++i) {
+        const dfq_csr& g = graphs[i];
+        if (g.n < 1 || g.e < 0 || !g.offsets || (g.e > 0 && !g.cols) || g.offsets[0] != 0 || g.offsets[g.n] != g.e) {
+            pool_release(p);
+            return fail(DFQ_EFORMAT, "pool graph %d is not a valid CSR", i);
+        }
+        for (int32_t u = 0; u < g.n; ++u)
+            if (g.offsets[u + 1] < g.offsets[u]) { pool_release(p); return fail(DFQ_EFORMAT, "graph %d: offsets decrease", i); }
+        for (int64_t k = 0; k < g.e; ++k)
+            if ((uint32_t)g.cols[k] >= (uint32_t)g.n) { pool_release(p); return fail(DFQ_EFORMAT, "graph %d: column out of range", i); }
+        p->n.push_back(g.n);
+        p->e.push_back(g.e);
+        const bool wide = g.e >= o.wide_min_edges && g.e >= (int64_t)o.wide_min_degree * g.n;
+        p->wide.push_back(wide ? 1 : 0);
+        // narrow cost estimate: edges plus levels times a per-level latency
+        // in edge units; sparse graphs (average degree < 8) get ~2 sqrt(n) levels
+        const double deg = (double)g.e / g.n;
+        const double levels = deg < 8 ? 2.0 * std::sqrt((double)g.n) : std::log2((double)g.n + 2);
+        p->cost.push_back((double)g.e + 4096.0 * levels);
+        off_base[i] = tot_n;
+        col_base[i] = tot_e;
+        tot_n += (int64_t)g.n + 1;
+        tot_e += ((g.e + 3) & ~(int64_t)3) + kColsPad;
+    }
+#define P_TRY(x) do { int rc_ = (x); if (rc_) { pool_release(p); return rc_; } } while (0)
+#define P_CUDA(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { pool_release(p); return fail(DFQ_ECUDA, "%s: %s", #x, cudaGetErrorString(e_)); } } while (0)
+    P_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    P_CUDA(cudaEventCreate(&p->ev0));
+    P_CUDA(cudaEventCreate(&p->ev1));
+    P_TRY(dmalloc(&p->offsets, sizeof(int32_t) * (size_t)tot_n));
+    P_TRY(dmalloc(&p->cols, sizeof(int32_t) * (size_t)tot_e));
+    P_CUDA(cudaMemsetAsync(p->cols, 0, sizeof(int32_t) * (size_t)tot_e, p->stream));
+    for (int i = 0; i < ngraphs; ++i) {
+        const dfq_csr& g = graphs[i];
+        P_CUDA(cudaMemcpyAsync(p->offsets + off_base[i], g.offsets, sizeof(int32_t) * ((size_t)g.n + 1),
+                               cudaMemcpyHostToDevice, p->stream));
+        if (g.e) P_CUDA(cudaMemcpyAsync(p->cols + col_base[i], g.cols, sizeof(int32_t) * (size_t)g.e,
+                                        cudaMemcpyHostToDevice, p->stream));
+        PoolGraph pg;
+        pg.offsets = p->offsets + off_base[i];
+        pg.cols = p->cols + col_base[i];
+        pg.n = g.n;
+        pg.wide = p->wide[i];
+        pg.e = g.e;
+        p->h_graphs.push_back(pg);
+        P_CUDA(cudaStreamSynchronize(p->stream));  // host CSR may be pageable
+    }
+    P_TRY(dmalloc(&p->d_graphs, sizeof(PoolGraph) * ngraphs));
+    P_CUDA(cudaMemcpyAsync(p->d_graphs, p->h_graphs.data(), sizeof(PoolGraph) * ngraphs, cudaMemcpyHostToDevice,
+                           p->stream));
+    P_TRY(dmalloc(&p->d_misc, 256));
+    P_TRY(dmalloc(&p->d_t0, 256));
+    P_TRY(dmalloc(&p->d_ctl1, sizeof(Control)));
+    P_CUDA(cudaMallocHost((void**)&p->h_t0, 64));
+    P_CUDA(cudaMallocHost((void**)&p->h_ctl1, sizeof(Control)));
+    P_CUDA(cudaStreamSynchronize(p->stream));
+#undef P_TRY
+#undef P_CUDA
+    *out = p;
+    return DFQ_OK;
+}
+
+int dfq_pool_destroy(dfq_pool* p) {
+    clear_error();
+    if (!p) return fail(DFQ_EINVAL, "dfq_pool_destroy: null pool");
+    pool_release(p);
+    return DFQ_OK;
+}
+
+int32_t dfq_pool_num_graphs(const dfq_pool* p) { return p ? p->ngraphs : -1; }
+
+int dfq_pool_graph_info(const dfq_pool* p, int32_t graph, int32_t* n, int64_t* e, int32_t* wide) {
+    clear_error();
+    if (!p || graph < 0 || graph >= p->ngraphs) return fail(DFQ_EINVAL, "dfq_pool_graph_info: bad graph");
+    if (n) *n = p->n[graph];
+    if (e) *e = p->e[graph];
+    if (wide) *wide = p->wide[graph];
+    return DFQ_OK;
+}
+
+int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32_t* parents, dfq_stats* stats) {
+    clear_error();
+    if (!p || graph < 0 || graph >= p->ngraphs || !levels) return fail(DFQ_EINVAL, "dfq_pool_bfs: bad arguments");
+    if (src < 0 || src >= p->n[graph]) return fail(DFQ_EINVAL, "source %d outside [0,%d)", src, p->n[graph]);
+    cudaSetDevice(p->device);
+    const bool par = parents != nullptr;
+    int rc = ensure_wide(p, par);
+    if (rc) return rc;
+    const dfq_opts& o = p->opts;
+    const void* fn = pick_single(o.block_threads, par);
+    if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
+    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
+    int grid = 0;
+    if ((rc = grid_for(p, fn, o.block_threads, lay.bytes, &grid))) return rc;
+    const Workspace w = ws_from(p->wide_mem, p->wide_lay);
+    Params prm;
+    memset(&prm, 0, sizeof prm);
+    prm.offsets = p->h_graphs[graph].offsets;
+    prm.cols = p->h_graphs[graph].cols;
+    prm.n = p->n[graph];
+    prm.src = src;
+    prm.levels = levels;
+    prm.parents = parents;
+    prm.bitmap = w.bitmap;
+    prm.bitmap_words = (p->n[graph] + 31) / 32;
+    for (int i = 0; i < 2; ++i) {
+        prm.ovf[i] = w.ovf[i];
+        prm.ovfv[i] = w.ovfv[i];
+        prm.large[i] = w.large[i];
+        prm.piece_owner[i] = w.piece_owner[i];
+    }
+    prm.large_cap = w.large_cap;
+    prm.piece_cap = w.piece_cap;
+    prm.ctl = p->d_ctl1;
+    prm.medium_min = o.medium_min_degree;
+    prm.large_min = o.large_min_degree;
+    prm.piece_edges = o.piece_edges;
+    prm.local_cap = o.local_queue_cap;
+    prm.local_budget = o.local_edge_budget;
+    prm.probe_first = o.probe_first;
+    prm.use_tma = o.use_tma;
+    prm.timeout_ns = (long long)o.timeout_ms * 1000000LL;
+    cudaEventRecord(p->ev0, p->stream);
+    cudaMemsetAsync(p->d_ctl1, 0, sizeof(Control), p->stream);
+    if ((rc = launch_coop(fn, grid, o.block_threads, lay.bytes, &prm, p->stream))) return rc;
+    cudaEventRecord(p->ev1, p->stream);
+    cudaMemcpyAsync(p->h_ctl1, p->d_ctl1, sizeof(Control), cudaMemcpyDeviceToHost, p->stream);
+    cudaError_t err = cudaStreamSynchronize(p->stream);
+    if (err != cudaSuccess) return fail(DFQ_ECUDA, "dfq_pool_bfs: %s", cudaGetErrorString(err));
+    const Control& c = *p->h_ctl1;
+    if (stats) {
+        memset(stats, 0, sizeof *stats);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+        stats->kernel_ms = ms;
+        stats->depth = c.stats.depth;
+        stats->levels = c.stats.levels;
+        stats->reached = (int64_t)c.stats.claims + 1;
+        stats->edges = (int64_t)c.stats.edges;
+        stats->overflow = (int64_t)c.stats.overflow;
+        stats->large = (int64_t)c.stats.large;
+    }
+    return c.status ? fail(map_status(c.status), "dfq_pool_bfs: device status %d", c.status) : DFQ_OK;
+}
+
+int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, dfq_query_result* results,
+                   float* total_ms) {
+    clear_error();
+    if (!p || (nq > 0 && !q) || nq < 0) return fail(DFQ_EINVAL, "dfq_pool_batch: bad arguments");
+    if (nq == 0) { if (total_ms) *total_ms = 0; return DFQ_OK; }
+    cudaSetDevice(p->device);
+    const bool par = q[0].parents != nullptr;
+    for (int i = 0; i < nq; ++i) {
+        if (q[i].graph < 0 || q[i].graph >= p->ngraphs) return fail(DFQ_EINVAL, "query %d: graph %d", i, q[i].graph);
+        if (q[i].source < 0 || q[i].source >= p->n[q[i].graph]) return fail(DFQ_EINVAL, "query %d: source", i);
+        if (!q[i].levels) return fail(DFQ_EINVAL, "query %d: levels is null", i);
+        if ((q[i].parents != nullptr) != par) return fail(DFQ_EINVAL, "parents must be given for all queries or none");
+    }
+    const dfq_opts& o = p->opts;
+    const void* fn = pick_batch(o.block_threads, par);
+    if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
+    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
+    int grid = 0, rc;
+    if ((rc = grid_for(p, fn, o.block_threads, lay.bytes, &grid))) return rc;
+    if ((rc = ensure_wide(p, par))) return rc;
+    if ((rc = ensure_blocks(p, grid, par))) return rc;
+    if ((rc = ensure_tables(p, nq))) return rc;
+    // query table and lists (pinned staging, copied inside the launch sequence)
+    int nw = 0, nn = 0;
+    std::vector<int> narrow;
+    for (int i = 0; i < nq; ++i) {
+        BatchQuery& b = p->h_queries[i];
+        b.graph = q[i].graph;
+        b.source = q[i].source;
+        b.levels = q[i].levels;
+        b.parents = q[i].parents;
+        b.t_start = b.t_end = 0;
+        if (p->wide[q[i].graph]) p->h_lists[nw++] = i;
+        else narrow.push_back(i);
+    }
+    std::stable_sort(narrow.begin(), narrow.end(),
+                     [&](int a, int b) { return p->cost[q[a].graph] > p->cost[q[b].graph]; });
+    nn = (int)narrow.size();
+    for (int k = 0; k < nn; ++k) p->h_lists[nq + k] = narrow[k];
+
+    BatchParams bp;
+    memset(&bp, 0, sizeof bp);
+    bp.graphs = p->d_graphs;
+    bp.queries = p->d_queries;
+    bp.ctls = p->d_ctls;
+    bp.wide_list = p->d_lists;
+    bp.n_wide = nw;
+    bp.narrow_list = p->d_lists + nq;
+    bp.n_narrow = nn;
+    bp.narrow_next = p->d_misc;
+    bp.t0 = p->d_t0;
+    bp.wide_ws = ws_from(p->wide_mem, p->wide_lay);
+    bp.block_ws = p->block_mem;
+    bp.block_ws_stride = p->block_stride;
+    bp.block_lay = p->block_lay;
+    bp.medium_min = o.medium_min_degree;
+    bp.large_min = o.large_min_degree;
+    bp.piece_edges = o.piece_edges;
+    bp.local_cap = o.local_queue_cap;
+    bp.local_budget = o.local_edge_budget;
+    bp.probe_first = o.probe_first;
+    bp.use_tma = o.use_tma;
+    bp.timeout_ns = (long long)o.timeout_ms * 1000000LL;
+
+    auto enqueue = [&]() -> int {
+        cudaError_t e1 = cudaMemcpyAsync(p->d_queries, p->h_queries, sizeof(BatchQuery) * nq, cudaMemcpyHostToDevice, p->stream);
+        cudaError_t e2 = cudaMemcpyAsync(p->d_lists, p->h_lists, sizeof(int) * 2 * nq, cudaMemcpyHostToDevice, p->stream);
+        cudaError_t e3 = cudaMemsetAsync(p->d_ctls, 0, sizeof(Control) * nq, p->stream);
+        cudaError_t e4 = cudaMemsetAsync(p->d_misc, 0, 256, p->stream);
+        if (e1 || e2 || e3 || e4) return fail(DFQ_ECUDA, "batch upload failed");
+        return launch_coop(fn, grid, o.block_threads, lay.bytes, &bp, p->stream);
+    };
+    cudaEventRecord(p->ev0, p->stream);
+    if (flags & DFQ_BATCH_GRAPH) {
+        // the captured graph bakes in the kernel arguments: rebuild it when
+        // the batch's shape changes, else replay it with new table contents
+        if (!p->gexec || p->g_nq != nq || p->g_nwide != nw || p->g_par != (int)par) {
+            if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
+            cudaGraph_t graph = nullptr;
+            cudaError_t err = cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal);
+            if (err != cudaSuccess) return fail(DFQ_ECUDA, "begin capture: %s", cudaGetErrorString(err));
+            int erc = enqueue();
+            err = cudaStreamEndCapture(p->stream, &graph);
+            if (erc) { if (graph) cudaGraphDestroy(graph); return erc; }
+            if (err != cudaSuccess) return fail(DFQ_ECUDA, "end capture: %s", cudaGetErrorString(err));
+            err = cudaGraphInstantiate(&p->gexec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (err != cudaSuccess) { p->gexec = nullptr; return fail(DFQ_ECUDA, "instantiate: %s", cudaGetErrorString(err)); }
+            p->g_nq = nq;
+            p->g_nwide = nw;
+            p->g_par = par;
+        }
+        cudaError_t err = cudaGraphLaunch(p->gexec, p->stream);
+        if (err != cudaSuccess) return fail(DFQ_ECUDA, "graph launch: %s", cudaGetErrorString(err));
+    } else {
+        if ((rc = enqueue())) return rc;
+    }
+    cudaEventRecord(p->ev1, p->stream);
+    cudaMemcpyAsync(p->h_ctls, p->d_ctls, sizeof(Control) * nq, cudaMemcpyDeviceToHost, p->stream);
+    cudaMemcpyAsync(p->h_queries, p->d_queries, sizeof(BatchQuery) * nq, cudaMemcpyDeviceToHost, p->stream);
+    cudaMemcpyAsync(p->h_t0, p->d_t0, sizeof(long long), cudaMemcpyDeviceToHost, p->stream);
+    cudaError_t err = cudaStreamSynchronize(p->stream);
+    if (err != cudaSuccess) return fail(DFQ_ECUDA, "dfq_pool_batch: %s", cudaGetErrorString(err));
+    if (total_ms) cudaEventElapsedTime(total_ms, p->ev0, p->ev1);
+    int worst = DFQ_OK;
+    for (int i = 0; i < nq; ++i) {
+        const Control& c = p->h_ctls[i];
+        const int st = map_status(c.status);
+        if (st != DFQ_OK && worst == DFQ_OK) worst = st;
+        if (results) {
+            dfq_query_result& r = results[i];
+            r.status = st;
+            r.wide = p->wide[q[i].graph];
+            r.depth = c.stats.depth;
+            r.levels = c.stats.levels;
+            r.reached = (int64_t)c.stats.claims + 1;
+            r.edges = (int64_t)c.stats.edges;
+            r.start_us = (double)(p->h_queries[i].t_start - *p->h_t0) * 1e-3;
+            r.end_us = (double)(p->h_queries[i].t_end - *p->h_t0) * 1e-3;
+        }
+    }
+    return worst == DFQ_OK ? DFQ_OK : fail(worst, "dfq_pool_batch: at least one query failed on the device");
+}
+
+}  // extern "C"

@@ -216,10 +216,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 // global memory.  Returns false (all threads of the block) if the wait timed
 // out or another block reported an error.
 __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, long long timeout_ns,
-                                             int* s_flag, const LevelCtr* next, int* s_in) {
+                                             int* s_flag, const LevelCtr* next, int* s_in, int gsize) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        target += gridDim.x;
+        target += (unsigned)gsize;
         int ok = 1;
         red_add_release(&ctl->barrier, 1u);
         unsigned long long t0 = 0;
@@ -238,6 +238,30 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
             }
         }
         if (ok && *(volatile int*)&ctl->status != 0) ok = 0;
+        *s_flag = ok;
+        if (ok) {
+            s_in[0] = __ldcg(&next->pushed);
+            s_in[1] = __ldcg(&next->ovf_count);
+            const unsigned long long lp = __ldcg(&next->large_pack);
+            s_in[2] = (int)(lp >> 32);
+            s_in[3] = (int)(unsigned)lp;
+            s_in[4] = __ldcg(&next->pushed_edges);
+        }
+    }
+    __syncthreads();
+    return *s_flag != 0;
+}
+
+// Level barrier of a group of blocks running one BFS: the grid barrier above
+// for several blocks; for a one-block group, the block barrier plus thread 0
+// reading the counters its own block's atomics produced.
+__device__ __forceinline__ bool group_barrier(Control* ctl, int gsize, unsigned& target, long long timeout_ns,
+                                              int* s_flag, const LevelCtr* next, int* s_in) {
+    if (gsize > 1) return grid_barrier(ctl, target, timeout_ns, s_flag, next, s_in, gsize);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence_block();
+        const int ok = *(volatile int*)&ctl->status == 0;
         *s_flag = ok;
         if (ok) {
             s_in[0] = __ldcg(&next->pushed);
@@ -664,13 +688,23 @@ __device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tall
     }
 }
 
+// Per-warp state that outlives one BFS within a launch: the parity of each
+// of the warp's two mbarriers, and whether a bulk copy ever failed to land.
+struct WarpState {
+    unsigned phase_bits;
+    bool failed;
+};
+
+// One whole BFS (init, levels, statistics) run by a group of `gsize` blocks;
+// this block is number `grank` of the group.  The group is the whole grid of
+// a cooperative launch, or a single block.  Block-collective.
 template <int B, bool PAR>
-__global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_constant__ Params p) {
+__device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, WarpState& ws) {
     constexpr int NW = B / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // grid-wide warp index, interleaved across blocks so that consecutive
+    // group-wide warp index, interleaved across blocks so that consecutive
     // statically assigned chunks land on different SMs
-    const int gwarp = warp * (int)gridDim.x + (int)blockIdx.x, nwarps = (int)gridDim.x * NW;
+    const int gwarp = warp * gsize + grank, nwarps = gsize * NW;
     const SmemLayout lay = smem_layout(B, p.local_cap, p.piece_edges, PAR);
     const int P = p.piece_edges;
     int* wl = reinterpret_cast<int*>(dfq_smem + lay.wl_off) + warp * 96;
@@ -685,8 +719,8 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
     // ---- init: levels, parents, bitmap (source pre-set so no ordering is needed)
     const int src = p.src;
     {
-        const long long gtid = (long long)blockIdx.x * B + tid;
-        const long long nth = (long long)gridDim.x * B;
+        const long long gtid = (long long)grank * B + tid;
+        const long long nth = (long long)gsize * B;
         for (long long i = gtid; i < p.n; i += nth) {
             p.levels[i] = (i == src) ? 0 : -1;
             if (PAR) p.parents[i] = (i == src) ? src : -1;
@@ -718,29 +752,24 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
         sh.depth = 0;
         sh.overflow = sh.large = 0ull;
     }
-    if (lane == 0) {
-        mbar_init(&wbar[0], 1);
-        mbar_init(&wbar[1], 1);
-        mbar_fence_init();
-    }
-    unsigned phase_bits = 0;  // parity of the next completion of wbar[0], wbar[1]
+    unsigned& phase_bits = ws.phase_bits;  // parity of the next completion of wbar[0], wbar[1]
+    bool& warp_failed = ws.failed;
     unsigned bar_target = 0;
     int cur = 0;
     int L = 0;
     Tally t{0u, 0u};
-    bool warp_failed = false;
 
-    bool ok = grid_barrier(ctl, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[0], sh.in);
+    bool ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[0], sh.in);
 
     for (; ok; ++L) {
         const int pushed = sh.in[0];
-        if (blockIdx.x == 0 && tid == 0 && L < kTraceLevels) {
+        if (grank == 0 && tid == 0 && L < kTraceLevels) {
             ctl->trace_ns[L] = (long long)globaltimer();
             ctl->trace_frontier[L] = pushed;
         }
         if (pushed == 0) break;
         LevelCtr* cin = &ctl->lv[L % 3];
-        if (blockIdx.x == 0 && tid == 0) {
+        if (grank == 0 && tid == 0) {
             LevelCtr* cz = &ctl->lv[(L + 2) % 3];
             cz->ovf_count = 0;
             cz->ovf_grab = 0;
@@ -760,7 +789,7 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
         {
             // a block keeps at most about twice its fair share of a frontier
             // of this level's size; the rest is shared through the global queue
-            const int share = (pushed + (int)gridDim.x - 1) / (int)gridDim.x;
+            const int share = (pushed + gsize - 1) / gsize;
             lv.cap = min(p.local_cap, max(32, 2 * share));
         }
         // probe-then-claim where the level scans many edges (most of them hit
@@ -921,7 +950,7 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
             sh.ovf_edges = sh.large_edges = 0;
         }
         cur ^= 1;
-        ok = grid_barrier(ctl, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in);
+        ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in);
     }
 
     // ---- statistics
@@ -944,8 +973,31 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
         atomicAdd(&ctl->stats.overflow, sh.overflow);
         atomicAdd(&ctl->stats.large, sh.large);
         if (sh.depth) atomicMax(&ctl->stats.depth, sh.depth);
-        if (blockIdx.x == 0) ctl->stats.levels = L;
+        if (grank == 0) ctl->stats.levels = L;
     }
+    __syncthreads();
+    return ok || *(volatile int*)&ctl->status == 0;
+}
+
+// Per-warp mbarriers, initialised once per launch.
+template <int B, bool PAR>
+__device__ __forceinline__ void init_warp_barriers(int local_cap, int piece) {
+    const SmemLayout lay = smem_layout(B, local_cap, piece, PAR);
+    unsigned long long* wbar = reinterpret_cast<unsigned long long*>(dfq_smem + lay.bar_off) + (threadIdx.x >> 5) * 2;
+    if ((threadIdx.x & 31) == 0) {
+        mbar_init(&wbar[0], 1);
+        mbar_init(&wbar[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+}
+
+// Single-source BFS: the whole grid of a cooperative launch is one group.
+template <int B, bool PAR>
+__global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_constant__ Params p) {
+    init_warp_barriers<B, PAR>(p.local_cap, p.piece_edges);
+    WarpState ws{0u, false};
+    bfs_run<B, PAR>(p, (int)gridDim.x, (int)blockIdx.x, ws);
 }
 
 }  // namespace dfqk

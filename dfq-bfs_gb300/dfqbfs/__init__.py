@@ -38,7 +38,10 @@ EXPORTS = [
     "dfq_graph_set_opts", "dfq_graph_stream", "dfq_graph_num_vertices", "dfq_graph_num_edges",
     "dfq_bfs", "dfq_bfs_launch", "dfq_graph_sync", "dfq_bfs_last_stats", "dfq_autotune",
     "dfq_bfs_noalloc", "dfq_bfs_last_trace",
+    "dfq_pool_create", "dfq_pool_destroy", "dfq_pool_num_graphs", "dfq_pool_graph_info", "dfq_pool_bfs",
+    "dfq_pool_batch",
 ]
+BATCH_GRAPH = 1
 
 
 class DfqError(RuntimeError):
@@ -59,10 +62,20 @@ class Opts(C.Structure):
                 ("local_queue_cap", C.c_int32), ("local_edge_budget", C.c_int32),
                 ("piece_edges", C.c_int32),
                 ("probe_first", C.c_int32), ("l2_persist", C.c_int32),
-                ("use_tma", C.c_int32), ("timeout_ms", C.c_int32)]
+                ("use_tma", C.c_int32), ("timeout_ms", C.c_int32),
+                ("wide_min_edges", C.c_int32), ("wide_min_degree", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Query(C.Structure):
+    _fields_ = [("graph", C.c_int32), ("source", C.c_int32), ("levels", C.c_void_p), ("parents", C.c_void_p)]
+
+
+class QueryResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("wide", C.c_int32), ("depth", C.c_int32), ("levels", C.c_int32),
+                ("reached", C.c_int64), ("edges", C.c_int64), ("start_us", C.c_double), ("end_us", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -118,6 +131,17 @@ def lib() -> C.CDLL:
     L.dfq_graph_sync.argtypes = [C.c_void_p]
     L.dfq_bfs_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     L.dfq_autotune.argtypes = [C.c_void_p, P32, C.c_int32, C.POINTER(Opts)]
+    L.dfq_pool_create.argtypes = [C.POINTER(_Csr), C.c_int32, C.POINTER(Opts), C.POINTER(C.c_void_p)]
+    L.dfq_pool_destroy.argtypes = [C.c_void_p]
+    L.dfq_pool_num_graphs.argtypes = [C.c_void_p]
+    L.dfq_pool_num_graphs.restype = C.c_int32
+    L.dfq_pool_graph_info.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int32)]
+    L.dfq_pool_bfs.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(Stats)]
+    L.dfq_pool_batch.argtypes = [C.c_void_p, C.POINTER(Query), C.c_int32, C.c_int32, C.POINTER(QueryResult),
+                                 C.POINTER(C.c_float)]
+    for name in ("dfq_pool_create", "dfq_pool_destroy", "dfq_pool_graph_info", "dfq_pool_bfs", "dfq_pool_batch"):
+        getattr(L, name).restype = C.c_int
     L.dfq_bfs_last_trace.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32]
     L.dfq_bfs_last_trace.restype = C.c_int
     L.dfq_bfs_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_int32, C.c_void_p,
@@ -348,3 +372,59 @@ def bfs_noalloc(offsets_dev, cols_dev, n: int, e: int, source: int, levels_dev, 
                                 _ptr(levels_dev), _ptr(parents_dev) if parents_dev is not None else None,
                                 stream or None, C.byref(st)))
     return st
+
+
+class Pool:
+    """Device-resident pool of graphs (dfq_pool_create) with batched BFS."""
+
+    def __init__(self, graphs: list, opts: Opts | None = None):
+        self._keep = graphs
+        arr = (_Csr * len(graphs))()
+        for i, g in enumerate(graphs):
+            arr[i] = g._as_c()
+        h = C.c_void_p()
+        check(lib().dfq_pool_create(arr, len(graphs), C.byref(opts) if opts is not None else None, C.byref(h)))
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            check(lib().dfq_pool_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self, graph: int):
+        n, e, w = C.c_int32(), C.c_int64(), C.c_int32()
+        check(lib().dfq_pool_graph_info(self.h, graph, C.byref(n), C.byref(e), C.byref(w)))
+        return n.value, e.value, bool(w.value)
+
+    def bfs(self, graph: int, source: int, levels_dev, parents_dev=None) -> Stats:
+        st = Stats()
+        check(lib().dfq_pool_bfs(self.h, graph, source, _ptr(levels_dev),
+                                 _ptr(parents_dev) if parents_dev is not None else None, C.byref(st)))
+        return st
+
+    def batch(self, queries, flags: int = 0, check_status: bool = True):
+        """queries: list of (graph, source, levels_dev[, parents_dev]).
+        Returns (list of QueryResult, total device ms)."""
+        qa = (Query * len(queries))()
+        for i, q in enumerate(queries):
+            qa[i].graph, qa[i].source = int(q[0]), int(q[1])
+            qa[i].levels = _ptr(q[2])
+            qa[i].parents = _ptr(q[3]) if len(q) > 3 and q[3] is not None else None
+        res = (QueryResult * len(queries))()
+        ms = C.c_float()
+        rc = lib().dfq_pool_batch(self.h, qa, len(queries), flags, res, C.byref(ms))
+        if check_status:
+            check(rc)
+        return list(res), ms.value

@@ -136,6 +136,8 @@ typedef struct dfq_opts {
     int32_t l2_persist;         /* 1: visited bitmap in an L2 persisting access window */
     int32_t use_tma;            /* 1: stage large-bin pieces into smem with cp.async.bulk */
     int32_t timeout_ms;         /* bound on every device-side wait (0 = 5000) */
+    int32_t wide_min_edges;     /* pools: a graph runs on the whole grid when it has at least */
+    int32_t wide_min_degree;    /*   this many edges and this average degree (0 = defaults) */
 } dfq_opts;
 
 typedef struct dfq_stats {
@@ -205,6 +207,58 @@ int dfq_bfs_last_trace(dfq_graph* g, int64_t* start_ns, int32_t* frontier, int32
 /* Choose opts for this graph by timing candidate settings on a few sources;
  * writes the winner to *best and installs it on the graph. */
 int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, dfq_opts* best);
+
+/* ------------------------------------------- graph pools and batched BFS */
+/* No reference counterpart: the reference runs one source per process launch
+ * (its '$' mode re-queries one source at a time, DFQ:202-214,302-308).
+ *
+ * A pool holds many graphs resident on the device (their CSR arrays packed in
+ * two allocations) plus the BFS workspaces.  A batch runs many queries
+ * (graph, source) in ONE persistent cooperative launch: "wide" queries (graphs
+ * with at least wide_min_edges edges and average degree >= wide_min_degree)
+ * run one after another on the whole grid, then every block pulls "narrow"
+ * queries (small or high-diameter graphs) and runs each alone with its block
+ * barrier as the level barrier. */
+typedef struct dfq_pool dfq_pool;
+
+typedef struct dfq_query {
+    int32_t  graph;     /* index into the pool */
+    int32_t  source;
+    int32_t* levels;    /* device array of the graph's n entries (required) */
+    int32_t* parents;   /* device array or null; all queries of a batch or none */
+} dfq_query;
+
+typedef struct dfq_query_result {
+    int32_t status;     /* DFQ_OK or a DFQ_E* code of this query */
+    int32_t wide;       /* 1: ran on the whole grid, 0: on one block */
+    int32_t depth;
+    int32_t levels;
+    int64_t reached;
+    int64_t edges;      /* E_R */
+    double  start_us;   /* device clock, from the start of the batch launch */
+    double  end_us;
+} dfq_query_result;
+
+#define DFQ_BATCH_GRAPH  1  /* capture table upload + reset + launch in a CUDA graph and replay it */
+
+/* Upload graphs (host CSR) into a device pool.  opts may be null; its
+ * wide_* fields choose how queries are split.  Replaces, for many graphs at
+ * once, DFQ:194-199,273-277. */
+int dfq_pool_create(const dfq_csr* graphs, int32_t ngraphs, const dfq_opts* opts, dfq_pool** out);
+int dfq_pool_destroy(dfq_pool* p);
+int32_t dfq_pool_num_graphs(const dfq_pool* p);
+int dfq_pool_graph_info(const dfq_pool* p, int32_t graph, int32_t* n, int64_t* e, int32_t* wide);
+
+/* One query as one plain cooperative launch on the whole grid (synchronous):
+ * the per-query baseline batches are compared with. */
+int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels_dev, int32_t* parents_dev,
+                 dfq_stats* stats);
+
+/* Run nq queries in one persistent launch (flags: DFQ_BATCH_GRAPH).  Fills
+ * results[nq] (nullable) and *total_ms (device time of the batch, nullable).
+ * Returns DFQ_OK if every query succeeded. */
+int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, dfq_query_result* results,
+                   float* total_ms);
 
 /* -------------------------------------------------- allocation-free BFS */
 /* No counterpart in the reference (its kernel uses static __device__ queues
