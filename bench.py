@@ -205,6 +205,107 @@ def run_reference(args, ws, rank, pg):
     return 0
 
 
+def c4_graphs(seed: int = 1, count: int = 256):
+    """Config 4's pool: 3/4 R-MAT (scale uniform in 10..20, edge factor 8, 16
+    or 32, symmetrised, deduplicated) and 1/4 grids (side log-uniform in
+    64..1024, 1% of edges deleted, largest component), each seeded by its
+    index.  Cached as binary CSR in DFQ_BENCH_CACHE (default /tmp)."""
+    import dfqbfs as d
+    rng = np.random.default_rng(seed)
+    cache = Path(os.environ.get("DFQ_BENCH_CACHE", "/tmp")) / f"dfq_c4_s{seed}"
+    cache.mkdir(parents=True, exist_ok=True)
+    specs = []
+    for i in range(count):
+        if i % 4 != 3:
+            specs.append(("rmat", int(rng.integers(10, 21)), int(rng.choice([8, 16, 32]))))
+        else:
+            specs.append(("grid", int(round(64 * 2 ** rng.uniform(0, 4))), 0))
+    graphs = []
+    for i, (kind, a, b) in enumerate(specs):
+        f = cache / f"g{i}_{kind}_{a}_{b}.bin"
+        if f.exists():
+            try:
+                graphs.append(d.load(f, "bin"))
+                continue
+            except d.DfqError:
+                pass
+        g = d.gen_rmat(a, b, seed=1000 + i) if kind == "rmat" else d.gen_grid(a, 0.01, seed=1000 + i)[0]
+        g.save(f, "bin")
+        graphs.append(g)
+    return graphs, specs
+
+
+def run_batch(args, torch, d):
+    """Config 4: 1024 queries (4 seeded sources per graph) over the 256-graph
+    pool in one persistent launch replayed from a CUDA graph, against the
+    same queries as one plain cooperative launch each."""
+    import oracle
+    t_gen = time.perf_counter()
+    graphs, specs = c4_graphs()
+    t_gen = time.perf_counter() - t_gen
+    # options: autotuned on the largest R-MAT graph of the pool
+    big = max((i for i, s in enumerate(specs) if s[0] == "rmat"), key=lambda i: graphs[i].e)
+    with d.Graph(graphs[big]) as tg:
+        opts = tg.autotune(graphs[big].pick_sources(4, seed=7))
+    pool = d.Pool(graphs, opts)
+    queries = []
+    for gi, g in enumerate(graphs):
+        for s in g.pick_sources(4, seed=gi):
+            queries.append((gi, int(s), torch.empty(g.n, dtype=torch.int32, device="cuda")))
+    nq = len(queries)
+    nwide = sum(1 for q in queries if pool.info(q[0])[2])
+    # batched: first call captures the CUDA graph; then timed replays
+    res, _ = pool.batch(queries, d.BATCH_GRAPH)
+    for _ in range(max(args.warmup - 1, 0)):
+        pool.batch(queries, d.BATCH_GRAPH)
+    batch_ms, ends = [], []
+    for _ in range(max(args.steps, 1)):
+        t0 = time.perf_counter()
+        res, dev_ms = pool.batch(queries, d.BATCH_GRAPH)
+        batch_ms.append((time.perf_counter() - t0) * 1e3)
+        ends.append(np.array([r.end_us for r in res]) / 1e3)
+    # spot-check parity of 32 queries of the last batch
+    rng = np.random.default_rng(3)
+    bad = 0
+    for k in rng.choice(nq, size=min(32, nq), replace=False):
+        gi, s, lv = queries[k]
+        want = oracle.bfs(graphs[gi].offsets, graphs[gi].cols, s)
+        bad += int(not np.array_equal(lv.cpu().numpy(), want))
+    edges = sum(r.edges for r in res)
+    # per-query plain launches, one after another
+    for q in queries[:8]:
+        pool.bfs(q[0], q[1], q[2])
+    t0 = time.perf_counter()
+    done, plain_dev = [], []
+    for q in queries:
+        st = pool.bfs(q[0], q[1], q[2])
+        plain_dev.append(st.kernel_ms)
+        done.append((time.perf_counter() - t0) * 1e3)
+    plain_total = done[-1]
+    bms = float(np.median(batch_ms))
+    lat = np.median(np.stack(ends), axis=0)
+    out = {"metric": "batched BFS queries/s (config 4: 1024 queries, 256 graphs)", "value": nq / (bms * 1e-3),
+           "unit": "queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": bms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+           "data": "synthetic (seeded)",
+           "config": {"workload": "batch_c4_256graphs_1024q", "graphs": len(graphs),
+                      "rmat": sum(1 for s in specs if s[0] == "rmat"), "grids": sum(1 for s in specs if s[0] == "grid"),
+                      "queries": nq, "wide_queries": nwide, "total_edges": int(sum(g.e for g in graphs)),
+                      "opts": opts.as_dict(), "gen_s": round(t_gen, 1), "cuda_graph": True},
+           "batched": {"queries_per_s": nq / (bms * 1e-3), "batch_ms_host": bms, "batch_ms_device": dev_ms,
+                       "gteps": edges / (bms * 1e-3) / 1e9, "p50_ms": float(np.percentile(lat, 50)),
+                       "p99_ms": float(np.percentile(lat, 99)), "parity_spot_check_mismatches": bad},
+           "per_query_plain": {"queries_per_s": nq / (plain_total * 1e-3), "total_ms": plain_total,
+                               "p50_ms": float(np.percentile(done, 50)), "p99_ms": float(np.percentile(done, 99)),
+                               "service_p50_ms": float(np.percentile(plain_dev, 50)),
+                               "service_p99_ms": float(np.percentile(plain_dev, 99))},
+           "speedup_qps": (nq / (bms * 1e-3)) / (nq / (plain_total * 1e-3)),
+           "latency_note": "latency = completion time after all 1024 queries are submitted at t=0"}
+    pool.close()
+    print(json.dumps(out))
+    return 0
+
+
 def grid_sources(orig, side: int, k_interior: int = 12, seed: int = 1):
     """Config-3 sources: the 4 corners of the full grid (nearest kept vertex if
     a corner left the largest component) and k seeded interior vertices."""
@@ -300,7 +401,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="dfq", choices=["dfq", "reference"])
-    ap.add_argument("--workload", default="rmat22", choices=["rmat22", "grid4096", "zipf262k"])
+    ap.add_argument("--workload", default="rmat22", choices=["rmat22", "grid4096", "zipf262k", "batch"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference GPU kernel")
     ap.add_argument("--no-secondary", action="store_true", help="skip the grid (config 3) secondary line")
@@ -318,6 +419,8 @@ def main():
     import torch
     import dfqbfs as d
     torch.cuda.set_device(local)
+    if args.workload == "batch":
+        return run_batch(args, torch, d) if rank == 0 else 0
     t_gen = time.perf_counter()
     g, all_srcs, cfg = workload_graph(args.workload, args.scale)
     t_gen = time.perf_counter() - t_gen
