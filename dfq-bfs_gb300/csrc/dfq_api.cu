@@ -220,6 +220,7 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     }
     p.large_cap = g->large_cap;
     p.piece_cap = g->piece_cap;
+    p.ovf_cap = g->n;
     p.ctl = g->ctl;
     p.medium_min = o.medium_min_degree;
     p.large_min = o.large_min_degree;

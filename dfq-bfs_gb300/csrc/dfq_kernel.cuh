@@ -96,8 +96,9 @@ struct Params {
     int* parents;  // null unless parents requested
     unsigned* bitmap;
     int bitmap_words;
-    int2* ovf[2];   // (start, degree) overflow entries, capacity n each
+    int2* ovf[2];   // (start, degree) overflow entries, ovf_cap each
     int* ovfv[2];   // their vertex ids (parents only)
+    int ovf_cap;    // n (a vertex is queued once per BFS) unless a bounded workspace says less
     int4* large[2]; // (start, degree, first piece, vertex), capacity large_cap
     int* piece_owner[2];  // piece -> large-queue slot, capacity piece_cap
     int large_cap;
@@ -413,11 +414,11 @@ __device__ __forceinline__ void push_local(const Params& p, const Lv& lv, unsign
         for (int j = 0; j < 4; ++j) {
             if (loc >> j & 1) {
                 const int gi = gbase + pos;
-                if (gi < p.n) {
+                if (gi < p.ovf_cap) {
                     ovf[gi] = make_int2(st[j], dg[j]);
                     if (PAR) ovfv[gi] = v[j];
                 } else {
-                    set_error(p.ctl, kErrQueueCap, gi, p.n);
+                    set_error(p.ctl, kErrQueueCap, gi, p.ovf_cap);
                 }
                 ++pos;
             }

@@ -181,6 +181,7 @@ extern "C" int dfq_bfs_noalloc(const int32_t* offsets, const int32_t* cols, int3
     }
     p.large_cap = sl.large_cap;
     p.piece_cap = sl.piece_cap;
+    p.ovf_cap = n;
     p.ctl = ctl;
     p.medium_min = o.medium_min_degree;
     p.large_min = o.large_min_degree;

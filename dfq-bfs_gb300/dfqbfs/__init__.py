@@ -39,7 +39,8 @@ EXPORTS = [
     "dfq_bfs", "dfq_bfs_launch", "dfq_graph_sync", "dfq_bfs_last_stats", "dfq_autotune",
     "dfq_bfs_noalloc", "dfq_bfs_last_trace",
     "dfq_pool_create", "dfq_pool_destroy", "dfq_pool_num_graphs", "dfq_pool_graph_info", "dfq_pool_bfs",
-    "dfq_pool_batch",
+    "dfq_pool_batch", "dfq_server_create", "dfq_server_submit", "dfq_server_poll", "dfq_server_levels",
+    "dfq_server_release", "dfq_server_pending", "dfq_server_destroy",
 ]
 BATCH_GRAPH = 1
 
@@ -76,6 +77,17 @@ class Query(C.Structure):
 class QueryResult(C.Structure):
     _fields_ = [("status", C.c_int32), ("wide", C.c_int32), ("depth", C.c_int32), ("levels", C.c_int32),
                 ("reached", C.c_int64), ("edges", C.c_int64), ("start_us", C.c_double), ("end_us", C.c_double)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("ring_capacity", C.c_int32), ("idle_ms", C.c_int32),
+                ("with_parents", C.c_int32), ("narrow_queue_cap", C.c_int32)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("tag", C.c_int64), ("status", C.c_int32), ("wide", C.c_int32),
+                ("depth", C.c_int32), ("retried", C.c_int32), ("reached", C.c_int64), ("edges", C.c_int64),
+                ("submit_us", C.c_double), ("done_us", C.c_double), ("device_us", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -141,6 +153,17 @@ def lib() -> C.CDLL:
     L.dfq_pool_batch.argtypes = [C.c_void_p, C.POINTER(Query), C.c_int32, C.c_int32, C.POINTER(QueryResult),
                                  C.POINTER(C.c_float)]
     for name in ("dfq_pool_create", "dfq_pool_destroy", "dfq_pool_graph_info", "dfq_pool_bfs", "dfq_pool_batch"):
+        getattr(L, name).restype = C.c_int
+    L.dfq_server_create.argtypes = [C.c_void_p, C.POINTER(ServerOpts), C.POINTER(C.c_void_p)]
+    L.dfq_server_submit.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.POINTER(C.c_int64)]
+    L.dfq_server_poll.argtypes = [C.c_void_p, C.POINTER(ServerResult), C.c_int32, C.POINTER(C.c_int32)]
+    L.dfq_server_levels.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+    L.dfq_server_release.argtypes = [C.c_void_p, C.c_int64]
+    L.dfq_server_pending.argtypes = [C.c_void_p]
+    L.dfq_server_pending.restype = C.c_int64
+    L.dfq_server_destroy.argtypes = [C.c_void_p]
+    for name in ("dfq_server_create", "dfq_server_submit", "dfq_server_poll", "dfq_server_levels",
+                 "dfq_server_release", "dfq_server_destroy"):
         getattr(L, name).restype = C.c_int
     L.dfq_bfs_last_trace.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32]
     L.dfq_bfs_last_trace.restype = C.c_int
@@ -428,3 +451,65 @@ class Pool:
         if check_status:
             check(rc)
         return list(res), ms.value
+
+
+class Server:
+    """Continuous-batching BFS server over a Pool (dfq_server_*)."""
+
+    def __init__(self, pool: Pool, hbm_budget_bytes: int = 0, ring_capacity: int = 0, idle_ms: int = 0,
+                 with_parents: bool = False, narrow_queue_cap: int = 0):
+        self.pool = pool
+        o = ServerOpts(hbm_budget_bytes, ring_capacity, idle_ms, int(with_parents), narrow_queue_cap)
+        h = C.c_void_p()
+        check(lib().dfq_server_create(pool.h, C.byref(o), C.byref(h)))
+        self.h = h
+        self._buf = (ServerResult * 4096)()
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            check(lib().dfq_server_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, graph: int, source: int, tag: int = 0) -> int:
+        rid = C.c_int64()
+        check(lib().dfq_server_submit(self.h, graph, source, tag, C.byref(rid)))
+        return rid.value
+
+    def poll(self) -> list:
+        cnt = C.c_int32()
+        check(lib().dfq_server_poll(self.h, self._buf, len(self._buf), C.byref(cnt)))
+        return [ServerResult.from_buffer_copy(self._buf[i]) for i in range(cnt.value)]
+
+    @property
+    def pending(self) -> int:
+        return lib().dfq_server_pending(self.h)
+
+    def levels(self, rid: int, n: int, parents: bool = False):
+        lv = np.empty(n, np.int32)
+        pa = np.empty(n, np.int32) if parents else None
+        check(lib().dfq_server_levels(self.h, rid, lv.ctypes.data, pa.ctypes.data if pa is not None else None))
+        return lv, pa
+
+    def release(self, rid: int) -> None:
+        check(lib().dfq_server_release(self.h, rid))
+
+    def drain(self, timeout_s: float = 60.0) -> list:
+        import time as _t
+        out, t0 = [], _t.time()
+        while self.pending > 0:
+            out += self.poll()
+            if _t.time() - t0 > timeout_s:
+                raise TimeoutError(f"{self.pending} requests still pending")
+        return out + self.poll()

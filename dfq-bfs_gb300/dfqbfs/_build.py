@@ -27,8 +27,8 @@ NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-co
                   "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
 
 HOST_SRCS = ["host_graph.cpp", "host_gen.cpp", "autotune.cpp"]
-CUDA_SRCS = ["dfq_api.cu", "dfq_noalloc.cu", "dfq_batch.cu"]
-HEADERS = ["common.hpp", "dfq_kernel.cuh"]
+CUDA_SRCS = ["dfq_api.cu", "dfq_noalloc.cu", "dfq_batch.cu", "dfq_serve.cu"]
+HEADERS = ["common.hpp", "dfq_kernel.cuh", "dfq_pool.cuh"]
 
 
 def _stale(out: Path, deps: list[Path]) -> bool:

@@ -260,6 +260,55 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels_dev, i
 int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, dfq_query_result* results,
                    float* total_ms);
 
+/* ------------------------------------------------------------- serving */
+/* No reference counterpart.  A server keeps a pool resident and serves a
+ * stream of single-source requests with continuous batching on the device:
+ * one persistent serving kernel claims requests as they are published (block
+ * by block for narrow graphs; the whole grid, between its blocks' own
+ * requests, for wide graphs), so requests that arrive while others run join
+ * the device work at once.  Each request gets its level array (and parents)
+ * from an HBM arena; a request is admitted when its arrays fit the arena's
+ * budget and a ring slot is free, else it waits in FIFO order.  The kernel
+ * leaves after idle_ms without work and is relaunched on the next request. */
+typedef struct dfq_server dfq_server;
+
+typedef struct dfq_server_opts {
+    int64_t hbm_budget_bytes;  /* arena for per-request outputs (0 = 1/4 of free HBM) */
+    int32_t ring_capacity;     /* requests on the device at once, power of two (0 = 4096) */
+    int32_t idle_ms;           /* serving kernel exits after this long without work (0 = 20) */
+    int32_t with_parents;      /* also produce parent arrays */
+    int32_t narrow_queue_cap;  /* per-block frontier capacity for narrow requests (0 = 1 << 20);
+                                  a request that outgrows it is rerun on the whole grid */
+} dfq_server_opts;
+
+typedef struct dfq_server_result {
+    int64_t id;
+    int64_t tag;
+    int32_t status;     /* DFQ_OK or DFQ_E* */
+    int32_t wide;       /* 1: ran on the whole grid */
+    int32_t depth;
+    int32_t retried;    /* 1: outgrew a block's queues and was rerun on the whole grid */
+    int64_t reached;
+    int64_t edges;
+    double  submit_us;  /* host clock, microseconds since the server was created */
+    double  done_us;    /* host clock when the completion was observed */
+    double  device_us;  /* device time of the BFS itself */
+} dfq_server_result;
+
+int dfq_server_create(dfq_pool* pool, const dfq_server_opts* opts, dfq_server** out);
+/* Queue a request (never blocks); *id identifies it in results. */
+int dfq_server_submit(dfq_server* s, int32_t graph, int32_t source, int64_t tag, int64_t* id);
+/* Admit what fits, (re)launch the serving kernel if needed, and return up to
+ * max completed results in *count. */
+int dfq_server_poll(dfq_server* s, dfq_server_result* out, int32_t max, int32_t* count);
+/* Copy a completed request's levels (and parents) to host memory. */
+int dfq_server_levels(dfq_server* s, int64_t id, int32_t* levels, int32_t* parents);
+/* Return a completed request's arrays to the arena. */
+int dfq_server_release(dfq_server* s, int64_t id);
+/* Requests submitted but not yet completed. */
+int64_t dfq_server_pending(const dfq_server* s);
+int dfq_server_destroy(dfq_server* s);
+
 /* -------------------------------------------------- allocation-free BFS */
 /* No counterpart in the reference (its kernel uses static __device__ queues
  * plus managed allocations made by main()).
