@@ -702,6 +702,10 @@ struct WarpState {
 template <int B, bool PAR>
 __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, WarpState& ws) {
     constexpr int NW = B / 32;
+    if (gsize < 1 || grank < 0 || grank >= gsize) {  // a caller bug: refuse rather than loop
+        if (threadIdx.x == 0) set_error(p.ctl, kErrQueueCap, gsize, grank);
+        return false;
+    }
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // group-wide warp index, interleaved across blocks so that consecutive
     // statically assigned chunks land on different SMs

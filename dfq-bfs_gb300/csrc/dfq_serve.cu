@@ -23,9 +23,11 @@
 #include "dfq_pool.cuh"
 
 #include <atomic>
+#include <cstddef>
 #include <chrono>
 #include <deque>
 #include <map>
+#include <thread>
 #include <unordered_map>
 
 using namespace dfq;
@@ -57,15 +59,22 @@ struct ServeHost {  // counters written by the host, mapped
     int pad;
 };
 
-struct ServeDev {  // device memory; persists across launches
+struct ServeDev {  // device memory
+    // persist across launches
     unsigned long long narrow_next;   // next narrow request to claim
     unsigned long long narrow_avail;  // block 0's copy of the host's narrow count
     unsigned long long gang_done;     // wide requests completed
-    long long gang;                   // wide request the gang runs, -1 none
+    // reset by the host before each launch (from `gang` on)
+    unsigned long long gang_word;     // (gang index << 32) | kGangOpen while joinable | members
     int exit;                         // 1: every block leaves
-    int error;                        // a worker gave up waiting
-    unsigned long long gang_exit;     // blocks that left a gang run (monotone)
+    int error;                        // a block gave up waiting (1 scheduler gone, 2 slot, 3 gang)
+    int narrow_active;                // blocks running a narrow request now
+    int gang_left;                    // members that finished the current gang run
+    unsigned long long gang_size;     // ((gang index + 1) << 32) | members, once the window closed
+                                      // (+1: the reset value 0 must not name gang 0)
 };
+constexpr unsigned long long kGangOpen = 0x80000000ull;
+constexpr unsigned long long kGangCount = 0x7fffffffull;
 
 struct ServeParams {
     const PoolGraph* graphs;
@@ -81,6 +90,10 @@ struct ServeParams {
     size_t block_ws_stride;
     WsLayout block_lay;
     int block_ovf_cap;
+    int* block_state;  // per block: (loop iterations << 4) | last action, for diagnosis
+    int narrow_limit;  // at most this many blocks run narrow requests at once
+    int gang_min;      // a gang forms once this many blocks joined ...
+    long long join_ns; // ... or its window has been open this long
     int medium_min, large_min, piece_edges, local_cap, local_budget, probe_first, use_tma;
     long long timeout_ns;
     long long idle_ns;
@@ -162,12 +175,44 @@ __device__ __forceinline__ void zero_ctl(Control* c, int tid, int nth) {
 
 enum : int { kActWait = 0, kActNarrow = 1, kActGang = 2, kActExit = 3, kActRetry = 4 };
 
+// Scheduler (block 0, thread 0): form the gang for wide request k.  Opens the
+// join window with itself as member 0, waits until gang_min members joined or
+// join_ns passed, closes the window atomically and publishes the size.
+// Returns the number of members.
+__device__ __forceinline__ int form_gang(const ServeParams& s, unsigned long long k) {
+    ServeDev* dev = s.dev;
+    *(volatile int*)&dev->gang_left = 0;
+    __threadfence();
+    *(volatile unsigned long long*)&dev->gang_word = (k << 32) | kGangOpen | 1ull;
+    __threadfence();
+    // close when every block joined, or when at least gang_min joined and no
+    // one else arrived for 3 us, or when the window has been open join_ns
+    const unsigned long long t0 = globaltimer();
+    const unsigned long long want = (unsigned long long)min(s.gang_min, (int)gridDim.x);
+    unsigned long long last_n = 1, t_last = t0;
+    while (true) {
+        const unsigned long long n = *(volatile unsigned long long*)&dev->gang_word & kGangCount;
+        const unsigned long long now = globaltimer();
+        if (n != last_n) { last_n = n; t_last = now; }
+        if (n >= gridDim.x) break;
+        if (n >= want && (long long)(now - t_last) > 3000) break;
+        if ((long long)(now - t0) > s.join_ns) break;
+    }
+    const unsigned long long old = atomicAnd(&dev->gang_word, ~kGangOpen);
+    const int m = (int)(old & kGangCount);
+    __threadfence();
+    *(volatile unsigned long long*)&dev->gang_size = ((k + 1) << 32) | (unsigned long long)m;
+    __threadfence();
+    return m;
+}
+
 template <int B, bool PAR>
 __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_constant__ ServeParams s) {
     __shared__ Params sp;
     __shared__ ServeReq s_req;
-    __shared__ int s_act;
+    __shared__ int s_act, s_rank, s_size;
     __shared__ long long s_k;
+    __shared__ unsigned long long s_next_gang;  // the first gang this block may still join
     init_warp_barriers<B, PAR>(s.local_cap, s.piece_edges);
     WarpState ws{0u, false};
     const int tid = threadIdx.x;
@@ -187,9 +232,6 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_con
         bw.large_cap = s.block_lay.large_cap;
         bw.piece_cap = s.block_lay.piece_cap;
     }
-
-    // the next wide request this block must join
-    __shared__ unsigned long long s_next_gang;
     if (tid == 0) s_next_gang = *(volatile unsigned long long*)&dev->gang_done;
     __syncthreads();
 
@@ -210,33 +252,60 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_con
                 if (a0 != last_a0 || a1 != last_a1 || nn != last_nn) idle_since = now;
                 last_a0 = a0; last_a1 = a1; last_nn = nn;
                 if (a1 > gd) {
-                    act = kActGang;
-                    s_k = (long long)gd;
                     zero_ctl(&s.ctls[1][gd & mask], 0, 1);
                     __threadfence();
-                    *(volatile long long*)&dev->gang = (long long)gd;
-                    __threadfence();
+                    s_size = form_gang(s, gd);
+                    s_rank = 0;
+                    s_k = (long long)gd;
+                    act = kActGang;
                 } else if (nn >= a0 && (stop || (long long)(now - idle_since) > s.idle_ns)) {
                     act = kActExit;
                     *(volatile int*)&dev->exit = 1;
                     __threadfence();
                 }
             } else {
-                // worker: join a gang, else claim a narrow request, else wait
-                const long long g = *(volatile long long*)&dev->gang;
-                if (g >= 0 && (unsigned long long)g >= s_next_gang) {
-                    act = kActGang;
-                    s_k = g;
+                // worker: join an open gang, else claim a narrow request (while
+                // fewer than narrow_limit blocks hold one), else wait
+                // one word names the gang and its window, so a join is tied to
+                // the gang the worker saw
+                const unsigned long long w = *(volatile unsigned long long*)&dev->gang_word;
+                const unsigned long long g = w >> 32;
+                bool handled = false;
+                if ((w & kGangOpen) && g >= s_next_gang) {
+                    handled = true;
+                    act = kActRetry;
+                    if (atomicCAS(&dev->gang_word, w, w + 1) == w) {
+                        // joined as member w & count; wait (bounded) for the size
+                        const unsigned long long t0 = globaltimer();
+                        unsigned long long sz;
+                        while (((sz = *(volatile unsigned long long*)&dev->gang_size) >> 32) != g + 1)
+                            if ((long long)(globaltimer() - t0) > s.timeout_ns) break;
+                        if ((sz >> 32) == g + 1 && (int)(unsigned)sz >= 1) {
+                            s_rank = (int)(w & kGangCount);
+                            s_size = (int)(unsigned)sz;
+                            s_k = (long long)g;
+                            act = kActGang;
+                        } else {
+                            atomicExch(&dev->error, 3);
+                            act = kActExit;
+                        }
+                    }
                     idle_since = globaltimer();
-                } else {
+                }
+                if (!handled) {
                     const unsigned long long nn = *(volatile unsigned long long*)&dev->narrow_next;
                     const unsigned long long av = *(volatile unsigned long long*)&dev->narrow_avail;
-                    if (nn < av) {
-                        if (atomicCAS(&dev->narrow_next, nn, nn + 1) == nn) {
-                            act = kActNarrow;
-                            s_k = (long long)nn;
+                    if (nn < av && *(volatile int*)&dev->narrow_active < s.narrow_limit) {
+                        act = kActRetry;
+                        if (atomicAdd(&dev->narrow_active, 1) < s.narrow_limit) {
+                            if (atomicCAS(&dev->narrow_next, nn, nn + 1) == nn) {
+                                act = kActNarrow;
+                                s_k = (long long)nn;
+                            } else {
+                                atomicSub(&dev->narrow_active, 1);
+                            }
                         } else {
-                            act = kActRetry;
+                            atomicSub(&dev->narrow_active, 1);
                         }
                         idle_since = globaltimer();
                     } else if (*(volatile int*)&dev->exit) {
@@ -253,10 +322,13 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_con
                 if (!read_req(&s.ring[r][(unsigned long long)s_k & mask], (unsigned long long)s_k, s_req,
                               s.timeout_ns)) {
                     atomicExch(&dev->error, 2);
+                    if (act == kActNarrow) atomicSub(&dev->narrow_active, 1);
                     act = kActExit;
                 }
             }
             s_act = act;
+            const int prev = s.block_state[blockIdx.x];
+            *(volatile int*)&s.block_state[blockIdx.x] = (((prev >> 4) + 1) << 4) | act;
         }
         __syncthreads();
         const int act = s_act;
@@ -272,21 +344,18 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_con
             if (tid == 0) serve_params(sp, s, s_req, s.wide_ws, s.wide_ovf_cap, &s.ctls[1][slot]);
             __syncthreads();
             const long long t0 = (long long)globaltimer();
-            bfs_run<B, PAR>(sp, (int)gridDim.x, (int)blockIdx.x, ws);
+            bfs_run<B, PAR>(sp, s_size, s_rank, ws);
             if (tid == 0) {
                 s_next_gang = k + 1;
-                // every block has added its statistics once it counts itself out
+                // a member's statistics are in once it counts itself out
                 __threadfence();
-                atomicAdd(&dev->gang_exit, 1ull);
+                atomicAdd(&dev->gang_left, 1);
                 if (blockIdx.x == 0) {
-                    const unsigned long long want = (k + 1) * (unsigned long long)gridDim.x;
                     const unsigned long long tw = globaltimer();
-                    while (*(volatile unsigned long long*)&dev->gang_exit < want)
+                    while (*(volatile int*)&dev->gang_left < s_size)
                         if ((long long)(globaltimer() - tw) > s.timeout_ns) { atomicExch(&dev->error, 3); break; }
                     __threadfence();
                     publish_done(&s.done[1][slot], k, &s.ctls[1][slot], t0, (long long)globaltimer());
-                    *(volatile long long*)&dev->gang = -1;
-                    __threadfence();
                     *(volatile unsigned long long*)&dev->gang_done = k + 1;
                     __threadfence();
                 }
@@ -297,7 +366,10 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_con
             __syncthreads();
             const long long t0 = (long long)globaltimer();
             bfs_run<B, PAR>(sp, 1, 0, ws);
-            if (tid == 0) publish_done(&s.done[0][slot], k, &s.ctls[0][slot], t0, (long long)globaltimer());
+            if (tid == 0) {
+                publish_done(&s.done[0][slot], k, &s.ctls[0][slot], t0, (long long)globaltimer());
+                atomicSub(&dev->narrow_active, 1);
+            }
         }
         __syncthreads();
     }
@@ -320,6 +392,7 @@ struct dfq_server {
     ServeHost* h_host = nullptr;
     ServeHost* d_host = nullptr;
     ServeDev* d_dev = nullptr;
+    int* d_block_state = nullptr;
     Control* d_ctls[2] = {nullptr, nullptr};
     // per-block workspaces for narrow requests
     unsigned char* block_mem = nullptr;
@@ -414,6 +487,7 @@ void server_release_all(dfq_server* s) {
     }
     if (s->h_host) cudaFreeHost(s->h_host);
     cudaFree(s->d_dev);
+    cudaFree(s->d_block_state);
     cudaFree(s->block_mem);
     cudaFree(s->arena);
     if (s->kernel_done) cudaEventDestroy(s->kernel_done);
@@ -441,6 +515,10 @@ int launch_serve(dfq_server* s) {
     sp.block_ws_stride = s->block_stride;
     sp.block_lay = s->block_lay;
     sp.block_ovf_cap = s->opts.narrow_queue_cap;
+    sp.block_state = s->d_block_state;
+    sp.gang_min = std::max(1, s->grid / 2);
+    sp.narrow_limit = std::max(1, s->grid - sp.gang_min);
+    sp.join_ns = 200000;
     sp.medium_min = o.medium_min_degree;
     sp.large_min = o.large_min_degree;
     sp.piece_edges = o.piece_edges;
@@ -450,9 +528,12 @@ int launch_serve(dfq_server* s) {
     sp.use_tma = o.use_tma;
     sp.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     sp.idle_ns = (long long)s->opts.idle_ms * 1000000LL;
-    // reset the per-launch flags; claim cursors persist across launches
-    struct { long long gang; int exit; int error; } reset = {-1, 0, 0};
-    cudaError_t err = cudaMemcpyAsync(&s->d_dev->gang, &reset, sizeof reset, cudaMemcpyHostToDevice, s->stream);
+    // reset the per-launch state; claim cursors persist across launches
+    ServeDev reset;
+    memset(&reset, 0, sizeof reset);
+    const size_t from = offsetof(ServeDev, gang_word);
+    cudaError_t err = cudaMemcpyAsync(reinterpret_cast<char*>(s->d_dev) + from, reinterpret_cast<char*>(&reset) + from,
+                                      sizeof(ServeDev) - from, cudaMemcpyHostToDevice, s->stream);
     if (err != cudaSuccess) return fail(DFQ_ECUDA, "serve reset: %s", cudaGetErrorString(err));
     void* args[] = {&sp};
     err = cudaLaunchCooperativeKernel(s->fn, dim3(s->grid), dim3(o.block_threads), args, s->smem, s->stream);
@@ -613,6 +694,8 @@ int dfq_server_create(dfq_pool* pool, const dfq_server_opts* opts, dfq_server** 
     memset(s->h_host, 0, sizeof(ServeHost));
     S_CUDA(cudaHostGetDevicePointer((void**)&s->d_host, s->h_host, 0));
     S_TRY(dmalloc(&s->d_dev, sizeof(ServeDev)));
+    S_TRY(dmalloc(&s->d_block_state, sizeof(int) * (size_t)s->grid));
+    S_CUDA(cudaMemset(s->d_block_state, 0, sizeof(int) * (size_t)s->grid));
     S_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     S_CUDA(cudaEventCreateWithFlags(&s->kernel_done, cudaEventDisableTiming));
     S_CUDA(cudaMemsetAsync(s->d_dev, 0, sizeof(ServeDev), s->stream));
@@ -696,10 +779,79 @@ int dfq_server_release(dfq_server* s, int64_t id) {
 
 int64_t dfq_server_pending(const dfq_server* s) { return s ? s->pending : -1; }
 
+int dfq_server_replay(dfq_server* s, const int32_t* graph, const int32_t* source, const double* arrival_us,
+                      int32_t n, const int32_t* keep, dfq_server_result* results) {
+    clear_error();
+    if (!s || n < 0 || (n > 0 && (!graph || !source || !arrival_us || !results)))
+        return fail(DFQ_EINVAL, "dfq_server_replay: bad arguments");
+    for (int32_t i = 0; i < n; ++i) {
+        if (graph[i] < 0 || graph[i] >= s->pool->ngraphs || source[i] < 0 || source[i] >= s->pool->n[graph[i]])
+            return fail(DFQ_EINVAL, "dfq_server_replay: request %d is out of range", i);
+        if (i && arrival_us[i] < arrival_us[i - 1]) return fail(DFQ_EINVAL, "arrival times must not decrease");
+    }
+    const double base = s->now_us();
+    std::vector<dfq_server_result> buf(1024);
+    int32_t next = 0, done = 0;
+    int rc = DFQ_OK;
+    while (done < n) {
+        const double now = s->now_us() - base;
+        while (next < n && arrival_us[next] <= now) {
+            int64_t id = 0;
+            if ((rc = dfq_server_submit(s, graph[next], source[next], next, &id))) return rc;
+            ++next;
+        }
+        int32_t got = 0;
+        if ((rc = dfq_server_poll(s, buf.data(), (int32_t)buf.size(), &got))) return rc;
+        for (int32_t j = 0; j < got; ++j) {
+            dfq_server_result r = buf[j];
+            const int64_t i = r.tag;
+            r.submit_us = arrival_us[i];
+            r.done_us -= base;
+            results[i] = r;
+            ++done;
+            if (!keep || !keep[i]) dfq_server_release(s, r.id);
+        }
+    }
+    return DFQ_OK;
+}
+
 int dfq_server_destroy(dfq_server* s) {
     clear_error();
     if (!s) return fail(DFQ_EINVAL, "dfq_server_destroy: null server");
     reinterpret_cast<std::atomic<int>*>(&s->h_host->stop)->store(1, std::memory_order_release);
+    cudaSetDevice(s->pool->device);
+    // the serving kernel leaves once it sees stop; wait for that, bounded
+    const auto t0 = std::chrono::steady_clock::now();
+    while (s->running) {
+        const cudaError_t q = cudaEventQuery(s->kernel_done);
+        if (q != cudaErrorNotReady) { s->running = false; break; }
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(10)) {
+            // report what every block was doing, read on a side stream while
+            // the kernel still runs; the server is left allocated
+            cudaStream_t side;
+            cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking);
+            ServeDev dv;
+            std::vector<int> st((size_t)s->grid);
+            cudaMemcpyAsync(&dv, s->d_dev, sizeof dv, cudaMemcpyDeviceToHost, side);
+            cudaMemcpyAsync(st.data(), s->d_block_state, sizeof(int) * st.size(), cudaMemcpyDeviceToHost, side);
+            cudaStreamSynchronize(side);
+            cudaStreamDestroy(side);
+            int hist[8] = {0};
+            for (int v : st) hist[v & 7]++;
+            fprintf(stderr,
+                    "dfq_server_destroy: serving kernel still running: narrow_next=%llu narrow_avail=%llu "
+                    "gang_done=%llu gang_word=%llx exit=%d error=%d narrow_active=%d gang_left=%d "
+                    "published=%llu/%llu; block actions wait=%d narrow=%d gang=%d exit=%d retry=%d; "
+                    "block0 state=%d iters=%d\n",
+                    (unsigned long long)dv.narrow_next, (unsigned long long)dv.narrow_avail,
+                    (unsigned long long)dv.gang_done, (unsigned long long)dv.gang_word, dv.exit, dv.error,
+                    dv.narrow_active, dv.gang_left, (unsigned long long)s->published[0],
+                    (unsigned long long)s->published[1], hist[0], hist[1], hist[2], hist[3], hist[4], st[0] & 15,
+                    st[0] >> 4);
+            return fail(DFQ_ETIMEOUT, "serving kernel did not stop within 10 s");
+        }
+        std::this_thread::sleep_for(std::chrono::milliseconds(1));
+    }
     server_release_all(s);
     return DFQ_OK;
 }

@@ -40,7 +40,7 @@ EXPORTS = [
     "dfq_bfs_noalloc", "dfq_bfs_last_trace",
     "dfq_pool_create", "dfq_pool_destroy", "dfq_pool_num_graphs", "dfq_pool_graph_info", "dfq_pool_bfs",
     "dfq_pool_batch", "dfq_server_create", "dfq_server_submit", "dfq_server_poll", "dfq_server_levels",
-    "dfq_server_release", "dfq_server_pending", "dfq_server_destroy",
+    "dfq_server_release", "dfq_server_pending", "dfq_server_destroy", "dfq_server_replay",
 ]
 BATCH_GRAPH = 1
 
@@ -162,6 +162,9 @@ def lib() -> C.CDLL:
     L.dfq_server_pending.argtypes = [C.c_void_p]
     L.dfq_server_pending.restype = C.c_int64
     L.dfq_server_destroy.argtypes = [C.c_void_p]
+    L.dfq_server_replay.argtypes = [C.c_void_p, P32, P32, C.POINTER(C.c_double), C.c_int32, P32,
+                                    C.POINTER(ServerResult)]
+    L.dfq_server_replay.restype = C.c_int
     for name in ("dfq_server_create", "dfq_server_submit", "dfq_server_poll", "dfq_server_levels",
                  "dfq_server_release", "dfq_server_destroy"):
         getattr(L, name).restype = C.c_int
@@ -504,6 +507,17 @@ class Server:
 
     def release(self, rid: int) -> None:
         check(lib().dfq_server_release(self.h, rid))
+
+    def replay(self, graphs, sources, arrival_us, keep=None) -> list:
+        """dfq_server_replay: submit request i at arrival_us[i]; returns results in request order."""
+        g = np.ascontiguousarray(graphs, np.int32)
+        s = np.ascontiguousarray(sources, np.int32)
+        a = np.ascontiguousarray(arrival_us, np.float64)
+        k = np.ascontiguousarray(keep, np.int32) if keep is not None else None
+        res = (ServerResult * len(g))()
+        check(lib().dfq_server_replay(self.h, _p32(g), _p32(s), a.ctypes.data_as(C.POINTER(C.c_double)), len(g),
+                                      _p32(k) if k is not None else None, res))
+        return list(res)
 
     def drain(self, timeout_s: float = 60.0) -> list:
         import time as _t

@@ -307,6 +307,17 @@ int dfq_server_levels(dfq_server* s, int64_t id, int32_t* levels, int32_t* paren
 int dfq_server_release(dfq_server* s, int64_t id);
 /* Requests submitted but not yet completed. */
 int64_t dfq_server_pending(const dfq_server* s);
+
+/* Replay a request trace: request i (graph[i], source[i]) is submitted at
+ * arrival_us[i] microseconds after the call starts (non-decreasing), the
+ * server is polled in between, and results[i] receives its result with
+ * submit_us = its scheduled arrival and done_us = when its completion was
+ * observed (both on the call's clock).  Results are released as they arrive
+ * unless keep (nullable) is non-zero for them; kept ones are released by the
+ * caller (dfq_server_levels / dfq_server_release with results[i].id).
+ * Returns after every request completed. */
+int dfq_server_replay(dfq_server* s, const int32_t* graph, const int32_t* source, const double* arrival_us,
+                      int32_t n, const int32_t* keep, dfq_server_result* results);
 int dfq_server_destroy(dfq_server* s);
 
 /* -------------------------------------------------- allocation-free BFS */

@@ -92,8 +92,9 @@ def test_admission_waits_for_hbm_budget():
     biggest = max(g.n for g in graphs)
     with d.Pool(graphs, pool_opts()) as pool, d.Server(pool, hbm_budget_bytes=4 * biggest * 3, idle_ms=50) as srv:
         reqs = {srv.submit(gi, s): (gi, s) for gi, s in requests(graphs, 60, seed=3)}
-        results = []
+        results, t0 = [], time.time()
         while srv.pending:
+            assert time.time() - t0 < 60, f"{srv.pending} requests still pending"
             got = srv.poll()
             results += got
             for r in got:  # free arena space as results are consumed
