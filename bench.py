@@ -205,14 +205,14 @@ def run_reference(args, ws, rank, pg):
     return 0
 
 
-def c4_graphs(seed: int = 1, count: int = 256):
-    """Config 4's pool: 3/4 R-MAT (scale uniform in 10..20, edge factor 8, 16
+def pool256_graphs(seed: int = 1, count: int = 256):
+    """The 256-graph batch pool: 3/4 R-MAT (scale uniform in 10..20, edge factor 8, 16
     or 32, symmetrised, deduplicated) and 1/4 grids (side log-uniform in
     64..1024, 1% of edges deleted, largest component), each seeded by its
     index.  Cached as binary CSR in DFQ_BENCH_CACHE (default /tmp)."""
     import dfqbfs as d
     rng = np.random.default_rng(seed)
-    cache = Path(os.environ.get("DFQ_BENCH_CACHE", "/tmp")) / f"dfq_c4_s{seed}"
+    cache = Path(os.environ.get("DFQ_BENCH_CACHE", "/tmp")) / f"dfq_pool256_s{seed}"
     cache.mkdir(parents=True, exist_ok=True)
     specs = []
     for i in range(count):
@@ -236,12 +236,12 @@ def c4_graphs(seed: int = 1, count: int = 256):
 
 
 def run_batch(args, torch, d):
-    """Config 4: 1024 queries (4 seeded sources per graph) over the 256-graph
+    """Batched workload: 1024 queries (4 seeded sources per graph) over the 256-graph
     pool in one persistent launch replayed from a CUDA graph, against the
     same queries as one plain cooperative launch each."""
     import oracle
     t_gen = time.perf_counter()
-    graphs, specs = c4_graphs()
+    graphs, specs = pool256_graphs()
     t_gen = time.perf_counter() - t_gen
     # options: autotuned on the largest R-MAT graph of the pool
     big = max((i for i, s in enumerate(specs) if s[0] == "rmat"), key=lambda i: graphs[i].e)
@@ -284,11 +284,11 @@ def run_batch(args, torch, d):
     plain_total = done[-1]
     bms = float(np.median(batch_ms))
     lat = np.median(np.stack(ends), axis=0)
-    out = {"metric": "batched BFS queries/s (config 4: 1024 queries, 256 graphs)", "value": nq / (bms * 1e-3),
+    out = {"metric": "batched BFS queries/s (1024 queries over 256 graphs)", "value": nq / (bms * 1e-3),
            "unit": "queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": bms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
            "data": "synthetic (seeded)",
-           "config": {"workload": "batch_c4_256graphs_1024q", "graphs": len(graphs),
+           "config": {"workload": "batch_256graphs_1024q", "graphs": len(graphs),
                       "rmat": sum(1 for s in specs if s[0] == "rmat"), "grids": sum(1 for s in specs if s[0] == "grid"),
                       "queries": nq, "wide_queries": nwide, "total_edges": int(sum(g.e for g in graphs)),
                       "opts": opts.as_dict(), "gen_s": round(t_gen, 1), "cuda_graph": True},
@@ -306,13 +306,13 @@ def run_batch(args, torch, d):
     return 0
 
 
-def c5_pool(target_gb: float = 40.0):
-    """Config 5's pool: R-MAT scales 16..24 (edge factor 16) and grids with
+def serve_pool(target_gb: float = 40.0):
+    """The serving pool: R-MAT scales 16..24 (edge factor 16) and grids with
     sides 1024, 2048, 4096 (1% deleted, largest component), each generated
     once and uploaded as many times as it takes to hold ~target_gb of CSR on
     the device (the copies are separate device graphs)."""
     import dfqbfs as d
-    cache = Path(os.environ.get("DFQ_BENCH_CACHE", "/tmp")) / "dfq_c5"
+    cache = Path(os.environ.get("DFQ_BENCH_CACHE", "/tmp")) / "dfq_serve_pool"
     cache.mkdir(parents=True, exist_ok=True)
     specs = [("rmat", s) for s in range(16, 25)] + [("grid", side) for side in (1024, 2048, 4096)]
     distinct = []
@@ -334,11 +334,11 @@ def c5_pool(target_gb: float = 40.0):
 
 
 def run_serve(args, torch, d):
-    """Config 5: Poisson request streams at swept rates over a ~40 GB resident
+    """Serving workload: Poisson request streams at swept rates over a ~40 GB resident
     pool, served by the continuous-batching server (trace replay in C++)."""
     import oracle
     t_gen = time.perf_counter()
-    distinct, specs, replicas, gb = c5_pool()
+    distinct, specs, replicas, gb = serve_pool()
     t_gen = time.perf_counter() - t_gen
     pool_graphs = [g for _ in range(replicas) for g in distinct]
     t_up = time.perf_counter()
@@ -381,11 +381,11 @@ def run_serve(args, torch, d):
     srv.close()
     pool.close()
     best = max(per_rate, key=lambda x: x["sustained_qps"])
-    out = {"metric": "BFS serving sustained queries/s (config 5, Poisson arrivals, ~40 GB pool)",
+    out = {"metric": "BFS serving sustained queries/s (Poisson arrivals, ~40 GB pool)",
            "value": best["sustained_qps"], "unit": "queries/s", "n_gpus": 1, "steps": len(rates), "warmup": 0,
            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
            "data": "synthetic (seeded)",
-           "config": {"workload": "serve_c5", "distinct_graphs": [f"{k}{a}" for k, a in specs],
+           "config": {"workload": "serve_poisson_40gb", "distinct_graphs": [f"{k}{a}" for k, a in specs],
                       "replicas": replicas, "pool_graphs": len(pool_graphs), "pool_gb": round(gb * replicas, 1),
                       "hbm_budget_gb": round(budget / 1e9, 1), "queries": "uniform over pool graphs, uniform "
                       "non-isolated sources", "gen_s": round(t_gen, 1), "upload_s": round(t_up, 1)},
@@ -395,7 +395,7 @@ def run_serve(args, torch, d):
 
 
 def grid_sources(orig, side: int, k_interior: int = 12, seed: int = 1):
-    """Config-3 sources: the 4 corners of the full grid (nearest kept vertex if
+    """Grid-workload sources: the 4 corners of the full grid (nearest kept vertex if
     a corner left the largest component) and k seeded interior vertices."""
     pos = {int(f): i for i, f in enumerate(orig)} if len(orig) < 1 << 22 else None
     lookup = (lambda f: pos.get(f)) if pos is not None else (
@@ -495,7 +495,7 @@ def main():
     ap.add_argument("--serve-max", type=int, default=4000, help="serve: cap on requests per rate")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference GPU kernel")
-    ap.add_argument("--no-secondary", action="store_true", help="skip the grid (config 3) secondary line")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the 4096^2 grid secondary line")
     ap.add_argument("--sources", type=int, default=64)
     ap.add_argument("--scale", type=int, default=22,
                     help="R-MAT scale (22 is the benchmark; smaller scales are for profiler captures)")
@@ -598,7 +598,7 @@ def main():
 
 
 def secondary_grid(torch, d, args):
-    """Config 3 (high diameter): GTEPS and microseconds per level on 4 of its
+    """The 4096^2 grid (high diameter): GTEPS and microseconds per level on 4 of its
     16 sources (2 corners, 2 interior), next to the reference kernel."""
     g, srcs, cfg = workload_graph("grid4096", 22)
     srcs = np.array([srcs[0], srcs[3], srcs[4], srcs[5]], np.int32)

@@ -9,13 +9,13 @@
 //     sniffed from the first byte; also the binary CSR cache (--save-bin).
 //   * source: the .dat header's (DFQ:188), or 0 for SNAP.  A numeric second
 //     argument overrides it (the reference ignores argv[2]; plot.py passes "8",
-//     R/plot.py:32 - give --ref-compat to ignore it the same way).
+//     plot.py:32 - give --ref-compat to ignore it the same way).
 //   * a last argument starting with '$' turns on the interactive loop: after
 //     each run "Exit? [y/n]" then "Source  : " read from stdin (DFQ:202-214,302-308).
 //   * stdout per run: "# Nodes : N", "# Edges : E", "Source  : S", "- Dist  = d",
 //     "- Touch = p % (r / N)", "- Error = k", "- Time  = <ms>ms" (DFQ:206-208,297-300),
 //     then "\033[0m" at exit (DFQ:311).  The time stays the second-to-last
-//     whitespace token, which is what plot.py parses (R/plot.py:33).
+//     whitespace token, which is what plot.py parses (plot.py:33).
 //   * "- Error" counts vertices whose level differs from a serial CPU BFS run
 //     by this program (the reference's self-check, DFQ:218-253,290-296); this
 //     program also counts vertices reached on the GPU but not on the CPU.

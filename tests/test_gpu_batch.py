@@ -1,4 +1,4 @@
-"""Graph pools and batched BFS (config 4's mechanism): many (graph, source)
+"""Graph pools and batched BFS: many (graph, source)
 queries in one persistent launch, wide queries on the whole grid and narrow
 ones one per block; every result bit-exact against the oracle, with and
 without CUDA-graph capture and replay, with parents, and per-query plain

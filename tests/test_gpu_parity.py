@@ -218,7 +218,7 @@ def test_autotune_keeps_parity():
 
 @pytest.mark.parametrize("cfg", ["rmat22", "grid4096"])
 def test_full_size_configs(cfg):
-    """Full-size RMAT-22 (config 2) and 4096^2 grid (config 3): bit-exact
+    """Full-size R-MAT scale 22 and the 4096^2 grid with 1% of edges deleted: bit-exact
     against the oracle for a few sources."""
     if cfg == "rmat22":
         g = d.gen_rmat(22, 16, seed=1)

@@ -1,4 +1,4 @@
-"""Serving (config 5's mechanism): continuous batching on the device.
+"""Serving: continuous batching on the device.
 
 Requests are submitted while others run; each result must be the same alone
 and in the mix - bit-exact levels (and valid parent trees) against the
