@@ -37,6 +37,28 @@ void parallel_for(int64_t n, F&& body, int64_t min_per_thread = 1 << 16) {
     for (auto& x : th) x.join();
 }
 
+// One run of an edge list: src[i] -> dst[i] for i in [0, m).
+struct EdgeSpan {
+    const int32_t* src;
+    const int32_t* dst;
+    int64_t m;
+};
+
+// CSR from the concatenation of `spans` (ids already in [0, n) are checked);
+// flags as for dfq_csr_from_edges.  Same result for any host thread count.
+int build_csr(const std::vector<EdgeSpan>& spans, int32_t n, int32_t flags, dfq_csr* out);
+
+// Run body(i) for i in [0, t) on t threads (the caller's thread takes i = 0).
+template <class F>
+void run_threads(int t, F&& body) {
+    if (t <= 1) { body(0); return; }
+    std::vector<std::thread> th;
+    th.reserve(t - 1);
+    for (int i = 1; i < t; ++i) th.emplace_back([&body, i] { body(i); });
+    body(0);
+    for (auto& x : th) x.join();
+}
+
 // SplitMix64 (Steele, Lea, Flood 2014): used to derive stream seeds.
 inline uint64_t splitmix64(uint64_t& s) {
     uint64_t z = (s += 0x9e3779b97f4a7c15ULL);

@@ -18,6 +18,12 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <new>
+
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 namespace dfq {
 
@@ -34,16 +40,32 @@ int fail(int code, const char* fmt, ...) {
 }
 void clear_error() { g_err.clear(); }
 
-int host_threads() {
-    static int t = [] {
+static std::atomic<int> g_threads{0};  // 0: DFQ_HOST_THREADS or the hardware count
+
+static int default_threads() {
+    static const int t = [] {
         const char* env = getenv("DFQ_HOST_THREADS");
         int v = env ? atoi(env) : 0;
         if (v <= 0) v = (int)std::thread::hardware_concurrency();
         if (v <= 0) v = 1;
-        if (v > 64) v = 64;
-        return v;
+        return v > 64 ? 64 : v;
     }();
     return t;
+}
+
+int host_threads() {
+    const int t = g_threads.load(std::memory_order_relaxed);
+    return t > 0 ? t : default_threads();
+}
+
+// Pieces to cut `units` of work into: with a thread count set explicitly,
+// that many (down to 16 units per piece, so small inputs still take the
+// parallel path); by default one piece per `min_per_piece` units, at most one
+// per host thread.
+static int pieces_for(int64_t units, int64_t min_per_piece) {
+    const int forced = g_threads.load(std::memory_order_relaxed);
+    const int64_t want = forced > 0 ? std::max<int64_t>(1, units / 16) : std::max<int64_t>(1, units / min_per_piece);
+    return (int)std::min<int64_t>(forced > 0 ? forced : default_threads(), want);
 }
 
 // ------------------------------------------------------------------ CSR build
@@ -90,6 +112,121 @@ static void dedup_rows(dfq_csr* g) {
     g->e = w;
 }
 
+// Parallel stable counting sort by row over an edge list given as consecutive
+// spans.  The list is cut into T chunks (whole spans when there are several,
+// equal slices of the one span otherwise); hist[c][v] counts the entries chunk
+// c adds to row v.  Row v receives chunk 0's entries first, then chunk 1's,
+// ..., each chunk in input order: exactly the order of one serial pass, so the
+// result does not depend on T.  T is bounded so the T x (n+1) histogram stays
+// <= 1 GiB, and raised so no chunk can count 2^31 entries into one row.
+int build_csr(const std::vector<EdgeSpan>& spans, int32_t n, int32_t flags, dfq_csr* out) {
+    memset(out, 0, sizeof *out);
+    const bool sym = flags & DFQ_CSR_SYMMETRIZE;
+    const bool noself = flags & DFQ_CSR_NO_SELF_LOOPS;
+    int64_t m = 0;
+    for (const EdgeSpan& sp : spans) m += sp.m;
+    const int64_t n1 = (int64_t)n + 1;
+    int64_t T = pieces_for(m, 1 << 16);
+    T = std::min<int64_t>(T, std::max<int64_t>(1, ((int64_t)1 << 28) / n1));
+    T = std::max<int64_t>(T, (m + ((int64_t)1 << 29) - 1) >> 29);
+    // chunk c = edges [cut[c], cut[c+1]) of the concatenated list
+    std::vector<int64_t> cut{0};
+    if (spans.size() > 1) {  // group whole spans, about m / T edges per chunk
+        int64_t at = 0;
+        for (size_t i = 0; i + 1 < spans.size(); ++i) {
+            at += spans[i].m;
+            if (at * T >= m * (int64_t)cut.size() && at > cut.back()) cut.push_back(at);
+        }
+        cut.push_back(m);
+        T = (int64_t)cut.size() - 1;
+    } else {
+        for (int64_t c = 1; c <= T; ++c) cut.push_back(m * c / T);
+    }
+    if (T < 1) T = 1, cut = {0, m};
+    // visit edges [lo, hi) of the concatenation in order
+    std::vector<int64_t> span_at{0};
+    for (const EdgeSpan& sp : spans) span_at.push_back(span_at.back() + sp.m);
+    auto for_edges = [&](int64_t lo, int64_t hi, auto&& f) {
+        size_t k = (size_t)(std::upper_bound(span_at.begin(), span_at.end(), lo) - span_at.begin()) - 1;
+        for (; lo < hi && k < spans.size(); ++k) {
+            const int64_t a = lo - span_at[k], b = std::min(hi, span_at[k + 1]) - span_at[k];
+            for (int64_t i = a; i < b; ++i) f(spans[k].src[i], spans[k].dst[i]);
+            lo = span_at[k + 1];
+        }
+    };
+    // validate ids: report the first bad edge in list order
+    std::vector<int64_t> bad((size_t)T, -1);
+    run_threads((int)T, [&](int c) {
+        int64_t i = cut[c];
+        bool found = false;
+        for_edges(cut[c], cut[c + 1], [&](int32_t u, int32_t v) {
+            if (!found && ((uint32_t)u >= (uint32_t)n || (uint32_t)v >= (uint32_t)n)) { bad[c] = i; found = true; }
+            ++i;
+        });
+    });
+    for (int64_t c = 0; c < T; ++c)
+        if (bad[c] >= 0) {
+            int32_t u = 0, v = 0;
+            for_edges(bad[c], bad[c] + 1, [&](int32_t a, int32_t b) { u = a; v = b; });
+            return fail(DFQ_EFORMAT, "edge %lld (%d -> %d) has an id outside [0, %d)", (long long)bad[c], u, v, n);
+        }
+    std::vector<uint32_t> hist;
+    try {
+        hist.assign((size_t)(T * n1), 0u);
+    } catch (const std::bad_alloc&) {
+        return fail(DFQ_ENOMEM, "CSR build: no host memory for a %lld x %lld histogram", (long long)T,
+                    (long long)n1);
+    }
+    run_threads((int)T, [&](int c) {
+        uint32_t* h = hist.data() + (size_t)c * n1;
+        for_edges(cut[c], cut[c + 1], [&](int32_t u, int32_t v) {
+            if (noself && u == v) return;
+            h[u]++;
+            if (sym) h[v]++;
+        });
+    });
+    std::vector<int64_t> deg((size_t)n1, 0);
+    parallel_for(n, [&](int64_t lo, int64_t hi) {
+        for (int64_t v = lo; v < hi; ++v) {
+            int64_t d = 0;
+            for (int64_t c = 0; c < T; ++c) d += hist[(size_t)(c * n1 + v)];
+            deg[v] = d;
+        }
+    });
+    int64_t total = 0;
+    for (int32_t u = 0; u < n; ++u) { int64_t d = deg[u]; deg[u] = total; total += d; }
+    deg[n] = total;
+    if (total >= ((int64_t)1 << 31))
+        return fail(DFQ_EINVAL, "graph has %lld directed edges; int32 offsets need < 2^31",
+                    (long long)total);
+    int rc = alloc_csr(n, total, out);
+    if (rc) return rc;
+    // hist[c][v] becomes the first position chunk c writes in row v
+    parallel_for(n1, [&](int64_t lo, int64_t hi) {
+        for (int64_t v = lo; v < hi; ++v) {
+            out->offsets[v] = (int32_t)deg[v];
+            uint32_t run = (uint32_t)deg[v];
+            for (int64_t c = 0; c < T; ++c) {
+                uint32_t& h = hist[(size_t)(c * n1 + v)];
+                const uint32_t k = h;
+                h = run;
+                run += k;
+            }
+        }
+    });
+    run_threads((int)T, [&](int c) {
+        uint32_t* pos = hist.data() + (size_t)c * n1;
+        int32_t* col = out->cols;
+        for_edges(cut[c], cut[c + 1], [&](int32_t u, int32_t v) {
+            if (noself && u == v) return;
+            col[pos[u]++] = v;
+            if (sym) col[pos[v]++] = u;
+        });
+    });
+    if (flags & DFQ_CSR_DEDUP) dedup_rows(out);
+    return DFQ_OK;
+}
+
 }  // namespace dfq
 
 using namespace dfq;
@@ -97,6 +234,15 @@ using namespace dfq;
 extern "C" {
 
 const char* dfq_last_error(void) { return g_err.c_str(); }
+
+int dfq_set_host_threads(int32_t threads) {
+    clear_error();
+    if (threads < 0 || threads > 256) return fail(DFQ_EINVAL, "dfq_set_host_threads: %d not in [0, 256]", threads);
+    g_threads.store(threads, std::memory_order_relaxed);
+    return DFQ_OK;
+}
+
+int32_t dfq_host_threads(void) { return host_threads(); }
 
 void dfq_free(void* p) { free(p); }
 
@@ -112,49 +258,7 @@ int dfq_csr_from_edges(const int32_t* src, const int32_t* dst, int64_t m, int32_
     clear_error();
     if (!out || (m > 0 && (!src || !dst)) || n < 0 || m < 0)
         return fail(DFQ_EINVAL, "dfq_csr_from_edges: bad arguments");
-    memset(out, 0, sizeof *out);
-    const bool sym = flags & DFQ_CSR_SYMMETRIZE;
-    const bool noself = flags & DFQ_CSR_NO_SELF_LOOPS;
-    // validate ids
-    std::atomic<int64_t> bad{-1};
-    parallel_for(m, [&](int64_t lo, int64_t hi) {
-        for (int64_t i = lo; i < hi; ++i)
-            if ((uint32_t)src[i] >= (uint32_t)n || (uint32_t)dst[i] >= (uint32_t)n) {
-                int64_t exp = -1;
-                bad.compare_exchange_strong(exp, i);
-                return;
-            }
-    });
-    if (bad.load() >= 0) {
-        int64_t i = bad.load();
-        return fail(DFQ_EFORMAT, "edge %lld (%d -> %d) has an id outside [0, %d)", (long long)i,
-                    src[i], dst[i], n);
-    }
-    std::vector<int64_t> deg((size_t)n + 1, 0);
-    for (int64_t i = 0; i < m; ++i) {
-        if (noself && src[i] == dst[i]) continue;
-        deg[src[i]]++;
-        if (sym) deg[dst[i]]++;
-    }
-    int64_t total = 0;
-    for (int32_t u = 0; u < n; ++u) { int64_t d = deg[u]; deg[u] = total; total += d; }
-    deg[n] = total;
-    if (total >= ((int64_t)1 << 31))
-        return fail(DFQ_EINVAL, "graph has %lld directed edges; int32 offsets need < 2^31",
-                    (long long)total);
-    int rc = alloc_csr(n, total, out);
-    if (rc) return rc;
-    for (int32_t u = 0; u <= n; ++u) out->offsets[u] = (int32_t)deg[u];
-    // stable fill: for each source, neighbours in input order (reverse edges
-    // interleave at the position of the edge that produced them)
-    for (int64_t i = 0; i < m; ++i) {
-        int32_t u = src[i], v = dst[i];
-        if (noself && u == v) continue;
-        out->cols[deg[u]++] = v;
-        if (sym) out->cols[deg[v]++] = u;
-    }
-    if (flags & DFQ_CSR_DEDUP) dedup_rows(out);
-    return DFQ_OK;
+    return build_csr({EdgeSpan{src, dst, m}}, n, flags, out);
 }
 
 }  // extern "C"
@@ -162,26 +266,45 @@ int dfq_csr_from_edges(const int32_t* src, const int32_t* dst, int64_t m, int32_
 // ------------------------------------------------------------------ text I/O
 namespace {
 
+// A whole input file: mapped read-only (text and binary parsers only read
+// it, every parser is bounded by p + n, nothing relies on a terminating NUL).
 struct Buf {
     char* p = nullptr;
     size_t n = 0;
-    ~Buf() { free(p); }
+    bool mapped = false;
+    ~Buf() {
+        if (mapped) munmap(p, n);
+        else free(p);
+    }
 };
 
 int read_file(const char* path, Buf& b) {
-    FILE* f = fopen(path, "rb");
-    if (!f) return fail(DFQ_EIO, "cannot open '%s': %s", path, strerror(errno));
-    if (fseek(f, 0, SEEK_END) != 0) { fclose(f); return fail(DFQ_EIO, "cannot seek '%s'", path); }
-    long sz = ftell(f);
-    if (sz < 0) { fclose(f); return fail(DFQ_EIO, "cannot size '%s'", path); }
-    fseek(f, 0, SEEK_SET);
-    b.p = (char*)malloc((size_t)sz + 1);
-    if (!b.p) { fclose(f); return fail(DFQ_ENOMEM, "cannot buffer %ld bytes of '%s'", sz, path); }
-    size_t got = fread(b.p, 1, (size_t)sz, f);
-    fclose(f);
-    if (got != (size_t)sz) return fail(DFQ_EIO, "short read on '%s'", path);
-    b.p[sz] = 0;
-    b.n = (size_t)sz;
+    const int fd = open(path, O_RDONLY);
+    if (fd < 0) return fail(DFQ_EIO, "cannot open '%s': %s", path, strerror(errno));
+    struct stat st;
+    if (fstat(fd, &st) != 0) { close(fd); return fail(DFQ_EIO, "cannot size '%s': %s", path, strerror(errno)); }
+    b.n = (size_t)st.st_size;
+    if (b.n > 0) {
+        void* m = mmap(nullptr, b.n, PROT_READ, MAP_PRIVATE, fd, 0);
+        if (m != MAP_FAILED) {
+            b.p = (char*)m;
+            b.mapped = true;
+            madvise(m, b.n, MADV_SEQUENTIAL);
+            close(fd);
+            return DFQ_OK;
+        }
+    }
+    // not mappable (empty file, special file): read it
+    b.p = (char*)malloc(b.n + 1);
+    if (!b.p) { close(fd); return fail(DFQ_ENOMEM, "cannot buffer %zu bytes of '%s'", b.n, path); }
+    size_t got = 0;
+    while (got < b.n) {
+        const ssize_t r = read(fd, b.p + got, b.n - got);
+        if (r <= 0) break;
+        got += (size_t)r;
+    }
+    close(fd);
+    if (got != b.n) return fail(DFQ_EIO, "short read on '%s'", path);
     return DFQ_OK;
 }
 
@@ -212,6 +335,45 @@ struct Cursor {
     void skip_line() { while (p < end && *p != '\n') ++p; if (p < end) ++p; }
 };
 
+// Cut [lo, hi) into at most t pieces whose boundaries sit on bytes for which
+// at(p) holds (a whitespace byte for token streams, the byte after '\n' for
+// line streams); returns t + 1 boundaries.
+template <class At>
+std::vector<const char*> split_text(const char* lo, const char* hi, int t, At at) {
+    std::vector<const char*> cut{lo};
+    const size_t len = (size_t)(hi - lo);
+    for (int i = 1; i < t; ++i) {
+        const char* q = lo + len * (size_t)i / (size_t)t;
+        if (q < cut.back()) q = cut.back();
+        while (q < hi && !at(q)) ++q;
+        cut.push_back(q);
+    }
+    cut.push_back(hi);
+    return cut;
+}
+
+inline int text_threads(size_t bytes) { return pieces_for((int64_t)bytes, 1 << 22); }
+
+// One whitespace-separated token as Cursor::next_int reads it: optional sign,
+// decimal digits, |value| <= 2^40.  false if it is not such an integer.
+inline bool token_int(const char* p, const char* e, int64_t& v) {
+    bool neg = false;
+    if (p < e && (*p == '-' || *p == '+')) { neg = (*p == '-'); ++p; }
+    if (p >= e) return false;
+    int64_t x = 0;
+    for (; p < e; ++p) {
+        if (*p < '0' || *p > '9') return false;
+        x = x * 10 + (*p - '0');
+        if (x > ((int64_t)1 << 40)) return false;
+    }
+    v = neg ? -x : x;
+    return true;
+}
+
+// .dat body after the header: N "start length" records, then E "dst x"
+// records.  Two parallel passes over the text: count tokens per piece, then
+// parse every token into its record slot.  Errors are reported for the first
+// bad record in file order, as a serial reader would.
 int parse_dat(const Buf& b, const char* path, dfq_csr* out) {
     Cursor c{b.p, b.p + b.n};
     int64_t n, e, s;
@@ -219,35 +381,92 @@ int parse_dat(const Buf& b, const char* path, dfq_csr* out) {
         return fail(DFQ_EFORMAT, "%s: .dat header must be 'N E SOURCE'", path);
     if (n < 0 || n >= ((int64_t)1 << 31) || e < 0 || e >= ((int64_t)1 << 31))
         return fail(DFQ_EFORMAT, "%s: header N=%lld E=%lld out of range", path, (long long)n, (long long)e);
-    std::vector<int32_t> start(n), len(n);
-    bool plain = true;  // rows already laid out back to back from 0?
-    int64_t run = 0;
-    for (int64_t i = 0; i < n; ++i) {
-        int64_t st, ln;
-        if (c.next_int(st) || c.next_int(ln))
-            return fail(DFQ_EFORMAT, "%s: node record %lld missing or malformed", path, (long long)i);
-        if (st < 0 || ln < 0 || st + ln > e)
+    std::vector<int32_t> start(n), len(n), edge(e > 0 ? e : 1);
+    const int64_t want = 2 * n + 2 * e;  // tokens after the header
+    const auto cut = split_text(c.p, c.end, text_threads((size_t)(c.end - c.p)),
+                                [](const char* q) { return is_space(*q); });
+    const int T = (int)cut.size() - 1;
+    std::vector<int64_t> base((size_t)T + 1, 0);
+    run_threads(T, [&](int t) {
+        int64_t k = 0;
+        for (const char* q = cut[t]; q < cut[t + 1];) {
+            while (q < cut[t + 1] && is_space(*q)) ++q;
+            if (q >= cut[t + 1]) break;
+            ++k;
+            while (q < cut[t + 1] && !is_space(*q)) ++q;
+        }
+        base[t + 1] = k;
+    });
+    for (int t = 0; t < T; ++t) base[t + 1] += base[t];
+    // first bad record in file order: node i -> key i, edge j -> key n + j
+    std::atomic<int64_t> bad_key{INT64_MAX};
+    auto note_bad = [&](int64_t key) {
+        int64_t cur = bad_key.load(std::memory_order_relaxed);
+        while (key < cur && !bad_key.compare_exchange_weak(cur, key)) {}
+    };
+    run_threads(T, [&](int t) {
+        int64_t k = base[t];
+        if (k >= want) return;
+        for (const char* q = cut[t]; q < cut[t + 1] && k < want; ++k) {
+            while (q < cut[t + 1] && is_space(*q)) ++q;
+            if (q >= cut[t + 1]) break;
+            const char* tok = q;
+            while (q < cut[t + 1] && !is_space(*q)) ++q;
+            int64_t v;
+            const bool ok = token_int(tok, q, v);
+            if (k < 2 * n) {
+                const int64_t i = k >> 1;
+                if (!ok || v < 0 || v > e) { note_bad(i); continue; }
+                if (k & 1) len[i] = (int32_t)v;
+                else start[i] = (int32_t)v;
+            } else {
+                const int64_t j = (k - 2 * n) >> 1;
+                if (!ok) { note_bad(n + j); continue; }
+                if (!((k - 2 * n) & 1)) {
+                    if (v < 0 || v >= n) { note_bad(n + j); continue; }
+                    edge[j] = (int32_t)v;
+                }
+            }
+        }
+    });
+    if (base[T] < want) note_bad(base[T] < 2 * n ? base[T] >> 1 : n + ((base[T] - 2 * n) >> 1));
+    // the start + length bound needs both fields of a record
+    parallel_for(n, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i)
+            if ((int64_t)start[i] + len[i] > e) { note_bad(i); return; }
+    });
+    const int64_t key = bad_key.load();
+    if (key != INT64_MAX) {
+        if (key < n) {
+            const int64_t t0 = 2 * key;
+            int64_t st = -1, ln = -1;
+            // re-read this record serially for the message
+            Cursor r{c.p, c.end};
+            for (int64_t k = 0; k < t0; ++k) { int64_t x; if (r.next_int(x)) break; }
+            const bool have = r.next_int(st) == 0 && r.next_int(ln) == 0;
+            if (!have)
+                return fail(DFQ_EFORMAT, "%s: node record %lld missing or malformed", path, (long long)key);
             return fail(DFQ_EFORMAT, "%s: node %lld has start=%lld length=%lld outside E=%lld", path,
-                        (long long)i, (long long)st, (long long)ln, (long long)e);
-        start[i] = (int32_t)st;
-        len[i] = (int32_t)ln;
-        if (st != run) plain = false;
-        run = st + ln;
-    }
-    if (run != e) plain = false;
-    std::vector<int32_t> edge(e > 0 ? e : 1);
-    for (int64_t i = 0; i < e; ++i) {
-        int64_t d, ignored;
-        if (c.next_int(d) || c.next_int(ignored))
-            return fail(DFQ_EFORMAT, "%s: edge record %lld missing or malformed", path, (long long)i);
-        if (d < 0 || d >= n)
-            return fail(DFQ_EFORMAT, "%s: edge %lld targets %lld outside [0,%lld)", path, (long long)i,
-                        (long long)d, (long long)n);
-        edge[i] = (int32_t)d;
+                        (long long)key, (long long)st, (long long)ln, (long long)e);
+        }
+        const int64_t j = key - n;
+        Cursor r{c.p, c.end};
+        bool have = true;
+        for (int64_t k = 0; k < 2 * n + 2 * j; ++k) { int64_t x; if (r.next_int(x)) { have = false; break; } }
+        int64_t d = 0, ignored = 0;
+        if (!have || r.next_int(d) || r.next_int(ignored))
+            return fail(DFQ_EFORMAT, "%s: edge record %lld missing or malformed", path, (long long)j);
+        return fail(DFQ_EFORMAT, "%s: edge %lld targets %lld outside [0,%lld)", path, (long long)j,
+                    (long long)d, (long long)n);
     }
     if (s < 0 || s >= n) s = 0;  // the reference re-prompts instead (DFQ:204-214)
     int64_t total = 0;
-    for (int64_t i = 0; i < n; ++i) total += len[i];
+    bool plain = true;  // rows already laid out back to back from 0?
+    for (int64_t i = 0; i < n; ++i) {
+        if (start[i] != total) plain = false;
+        total += len[i];
+    }
+    if (total != e) plain = false;
     int rc = alloc_csr((int32_t)n, total, out);
     if (rc) return rc;
     out->source = (int32_t)s;
@@ -256,8 +475,10 @@ int parse_dat(const Buf& b, const char* path, dfq_csr* out) {
     if (plain) {
         memcpy(out->cols, edge.data(), sizeof(int32_t) * total);
     } else {  // arbitrary (start, length) records: gather rows in vertex order
-        for (int64_t i = 0; i < n; ++i)
-            memcpy(out->cols + out->offsets[i], edge.data() + start[i], sizeof(int32_t) * len[i]);
+        parallel_for(n, [&](int64_t lo, int64_t hi) {
+            for (int64_t i = lo; i < hi; ++i)
+                memcpy(out->cols + out->offsets[i], edge.data() + start[i], sizeof(int32_t) * len[i]);
+        }, 1 << 12);
     }
     return DFQ_OK;
 }
@@ -274,47 +495,80 @@ bool parse_nodes_header(const char* p, const char* end, int64_t& n, int64_t& e) 
     const char* a = find("Nodes:");
     const char* b = find("Edges:");
     if (!a) return false;
-    n = strtoll(a, nullptr, 10);
-    e = b ? strtoll(b, nullptr, 10) : -1;
+    // bounded decimal read (the buffer is not NUL-terminated)
+    auto num = [&](const char* r) -> int64_t {
+        while (r < end && (*r == ' ' || *r == '\t')) ++r;
+        int64_t x = 0;
+        bool any = false;
+        while (r < end && *r >= '0' && *r <= '9' && x < ((int64_t)1 << 40)) { x = x * 10 + (*r++ - '0'); any = true; }
+        return any ? x : 0;
+    };
+    n = num(a);
+    e = b ? num(b) : -1;
     return true;
 }
 
+// SNAP edge list, parsed in parallel over line-aligned pieces of the text.
+// Each piece keeps its own edges, largest id, first "# Nodes:" header and first
+// error; pieces are then joined in file order, so the edge order, the header
+// taken and the error reported are those of a serial reader.
 int parse_snap(const Buf& b, const char* path, int32_t flags, dfq_csr* out) {
-    Cursor c{b.p, b.p + b.n};
-    int64_t hdr_n = -1, hdr_e = -1;
-    std::vector<int32_t> src, dst;
-    int64_t maxid = -1;
-    int64_t line = 0;
-    while (true) {
-        c.skip_space();
-        if (c.p >= c.end) break;
-        if (*c.p == '#') {
-            int64_t nn, ee;
-            if (hdr_n < 0 && parse_nodes_header(c.p, c.end, nn, ee)) {
-                hdr_n = nn;
-                hdr_e = ee;
-                if (hdr_e > 0 && hdr_e < ((int64_t)1 << 31)) { src.reserve(hdr_e); dst.reserve(hdr_e); }
+    const char* end = b.p + b.n;
+    const auto cut = split_text(b.p, end, text_threads(b.n), [&](const char* q) { return q > b.p && q[-1] == '\n'; });
+    const int T = (int)cut.size() - 1;
+    struct Piece {
+        std::vector<int32_t> src, dst;
+        int64_t maxid = -1, lines = 0, hdr_n = -1, hdr_e = -1;
+        int err = 0;  // 1: not 'FromNodeId ToNodeId', 2: id out of int32 range
+    };
+    std::vector<Piece> pc((size_t)T);
+    run_threads(T, [&](int t) {
+        Piece& P = pc[t];
+        P.src.reserve((size_t)(cut[t + 1] - cut[t]) / 10);
+        P.dst.reserve((size_t)(cut[t + 1] - cut[t]) / 10);
+        Cursor c{cut[t], cut[t + 1]};
+        while (true) {
+            c.skip_space();
+            if (c.p >= c.end) break;
+            if (*c.p == '#') {
+                int64_t nn, ee;
+                if (P.hdr_n < 0 && parse_nodes_header(c.p, c.end, nn, ee)) { P.hdr_n = nn; P.hdr_e = ee; }
+                c.skip_line();
+                continue;
             }
-            c.skip_line();
-            continue;
+            int64_t u, v;
+            ++P.lines;
+            if (c.next_int(u) || c.next_int(v)) { P.err = 1; return; }
+            if (u < 0 || v < 0 || u >= ((int64_t)1 << 31) - 1 || v >= ((int64_t)1 << 31) - 1) { P.err = 2; return; }
+            // anything after the two ids on the line (weights, timestamps) is ignored
+            while (c.p < c.end && *c.p != '\n') ++c.p;
+            P.src.push_back((int32_t)u);
+            P.dst.push_back((int32_t)v);
+            if (u > P.maxid) P.maxid = u;
+            if (v > P.maxid) P.maxid = v;
         }
-        int64_t u, v;
-        ++line;
-        if (c.next_int(u) || c.next_int(v))
-            return fail(DFQ_EFORMAT, "%s: edge line %lld is not 'FromNodeId ToNodeId'", path, (long long)line);
-        if (u < 0 || v < 0 || u >= ((int64_t)1 << 31) - 1 || v >= ((int64_t)1 << 31) - 1)
+    });
+    int64_t hdr_n = -1, lines = 0, maxid = -1, m = 0;
+    for (int t = 0; t < T; ++t) {
+        const Piece& P = pc[t];
+        if (P.err) {
+            const int64_t line = lines + P.lines;
+            if (P.err == 1)
+                return fail(DFQ_EFORMAT, "%s: edge line %lld is not 'FromNodeId ToNodeId'", path, (long long)line);
             return fail(DFQ_EFORMAT, "%s: edge line %lld has id out of int32 range", path, (long long)line);
-        // anything after the two ids on the line (weights, timestamps) is ignored
-        while (c.p < c.end && *c.p != '\n') ++c.p;
-        src.push_back((int32_t)u);
-        dst.push_back((int32_t)v);
-        if (u > maxid) maxid = u;
-        if (v > maxid) maxid = v;
+        }
+        if (hdr_n < 0 && P.hdr_n >= 0) hdr_n = P.hdr_n;
+        lines += P.lines;
+        maxid = std::max(maxid, P.maxid);
+        m += (int64_t)P.src.size();
     }
     int64_t n = hdr_n > 0 ? hdr_n : 0;
     if (maxid + 1 > n) n = maxid + 1;  // SNAP ids may exceed the header's count
     if (n >= ((int64_t)1 << 31)) return fail(DFQ_EFORMAT, "%s: too many vertices", path);
-    return dfq_csr_from_edges(src.data(), dst.data(), (int64_t)src.size(), (int32_t)n, flags, out);
+    std::vector<EdgeSpan> spans;
+    for (const Piece& P : pc)
+        if (!P.src.empty()) spans.push_back(EdgeSpan{P.src.data(), P.dst.data(), (int64_t)P.src.size()});
+    return build_csr(spans, (int32_t)n, flags, out);
 }
 
 int read_bin(const Buf& b, const char* path, dfq_csr* out) {
@@ -394,11 +648,15 @@ int dfq_csr_load(const char* path, int32_t format, int32_t flags, dfq_csr* out) 
     if (rc == DFQ_OK && (flags & (DFQ_CSR_SYMMETRIZE | DFQ_CSR_DEDUP | DFQ_CSR_NO_SELF_LOOPS))) {
         // re-run the edge list through the builder so flags mean the same for every format
         std::vector<int32_t> s(out->e), d(out->e);
-        for (int32_t u = 0; u < out->n; ++u)
-            for (int32_t k = out->offsets[u]; k < out->offsets[u + 1]; ++k) { s[k] = u; d[k] = out->cols[k]; }
+        const int32_t* off = out->offsets;
+        const int32_t* col = out->cols;
+        parallel_for(out->n, [&](int64_t lo, int64_t hi) {
+            for (int64_t u = lo; u < hi; ++u)
+                for (int32_t k = off[u]; k < off[u + 1]; ++k) { s[k] = (int32_t)u; d[k] = col[k]; }
+        }, 1 << 14);
         int32_t src = out->source, n = out->n;
         dfq_csr_free(out);
-        rc = dfq_csr_from_edges(s.data(), d.data(), (int64_t)s.size(), n, flags, out);
+        rc = build_csr({EdgeSpan{s.data(), d.data(), (int64_t)s.size()}}, n, flags, out);
         if (rc == DFQ_OK) out->source = src;
     }
     return rc;
@@ -418,27 +676,58 @@ int dfq_csr_save(const char* path, const dfq_csr* g, int32_t format) {
         if (g->e) memcpy(v.data() + 24 + 4 * ((size_t)g->n + 1), g->cols, 4 * (size_t)g->e);
         return write_all(path, v.data(), v.size());
     }
-    Out o;
-    o.v.reserve((size_t)g->e * 16 + (size_t)g->n * 16 + 128);
+    if (format != DFQ_FMT_SNAP && format != DFQ_FMT_DAT)
+        return fail(DFQ_EINVAL, "dfq_csr_save: unknown format %d", format);
+    // Text is formatted in parallel, one buffer per piece, and written in order.
+    const int T = pieces_for(g->e + g->n, 1 << 18);
+    std::vector<Out> part;
+    Out head;
     if (format == DFQ_FMT_SNAP) {
-        o.put("# Nodes: "); o.put_int(g->n); o.put(" Edges: "); o.put_int(g->e); o.ch('\n');
-        o.put("# FromNodeId\tToNodeId\n");
-        for (int32_t u = 0; u < g->n; ++u)
-            for (int32_t k = g->offsets[u]; k < g->offsets[u + 1]; ++k) {
-                o.put_int(u); o.ch('\t'); o.put_int(g->cols[k]); o.ch('\n');
-            }
-    } else if (format == DFQ_FMT_DAT) {
+        head.put("# Nodes: "); head.put_int(g->n); head.put(" Edges: "); head.put_int(g->e); head.ch('\n');
+        head.put("# FromNodeId\tToNodeId\n");
+        // pieces: vertex ranges holding about e / T edges each
+        std::vector<int32_t> vcut{0};
+        for (int t = 1; t < T; ++t) {
+            const int32_t want = (int32_t)(g->e * t / T);
+            const int32_t v = (int32_t)(std::lower_bound(g->offsets, g->offsets + g->n + 1, want) - g->offsets);
+            vcut.push_back(std::max(vcut.back(), std::min(v, g->n)));
+        }
+        vcut.push_back(g->n);
+        part.resize((size_t)T);
+        run_threads(T, [&](int t) {
+            Out& o = part[t];
+            o.v.reserve((size_t)(g->offsets[vcut[t + 1]] - g->offsets[vcut[t]]) * 16 + 64);
+            for (int32_t u = vcut[t]; u < vcut[t + 1]; ++u)
+                for (int32_t k = g->offsets[u]; k < g->offsets[u + 1]; ++k) {
+                    o.put_int(u); o.ch('\t'); o.put_int(g->cols[k]); o.ch('\n');
+                }
+        });
+    } else {
         // the second column of the edge records is ignored by the reference
         // loader (DFQ:199); it is written as 1
-        o.put_int(g->n); o.ch(' '); o.put_int(g->e); o.ch(' '); o.put_int(g->source); o.ch('\n');
-        for (int32_t u = 0; u < g->n; ++u) {
-            o.put_int(g->offsets[u]); o.ch(' '); o.put_int(g->offsets[u + 1] - g->offsets[u]); o.ch('\n');
-        }
-        for (int64_t k = 0; k < g->e; ++k) { o.put_int(g->cols[k]); o.put(" 1\n"); }
-    } else {
-        return fail(DFQ_EINVAL, "dfq_csr_save: unknown format %d", format);
+        head.put_int(g->n); head.ch(' '); head.put_int(g->e); head.ch(' '); head.put_int(g->source); head.ch('\n');
+        part.resize((size_t)(2 * T));
+        run_threads(T, [&](int t) {
+            Out& o = part[t];
+            const int32_t lo = (int32_t)((int64_t)g->n * t / T), hi = (int32_t)((int64_t)g->n * (t + 1) / T);
+            o.v.reserve((size_t)(hi - lo) * 20 + 64);
+            for (int32_t u = lo; u < hi; ++u) {
+                o.put_int(g->offsets[u]); o.ch(' '); o.put_int(g->offsets[u + 1] - g->offsets[u]); o.ch('\n');
+            }
+            Out& q = part[T + t];
+            const int64_t klo = g->e * t / T, khi = g->e * (t + 1) / T;
+            q.v.reserve((size_t)(khi - klo) * 12 + 64);
+            for (int64_t k = klo; k < khi; ++k) { q.put_int(g->cols[k]); q.put(" 1\n"); }
+        });
     }
-    return write_all(path, o.v.data(), o.v.size());
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(DFQ_EIO, "cannot create '%s': %s", path, strerror(errno));
+    bool ok = fwrite(head.v.data(), 1, head.v.size(), f) == head.v.size();
+    for (const Out& o : part)
+        if (ok && !o.v.empty()) ok = fwrite(o.v.data(), 1, o.v.size(), f) == o.v.size();
+    const int cl = fclose(f);
+    if (!ok || cl != 0) return fail(DFQ_EIO, "short write on '%s'", path);
+    return DFQ_OK;
 }
 
 }  // extern "C"

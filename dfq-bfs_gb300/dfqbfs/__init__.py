@@ -41,6 +41,7 @@ EXPORTS = [
     "dfq_pool_create", "dfq_pool_destroy", "dfq_pool_num_graphs", "dfq_pool_graph_info", "dfq_pool_bfs",
     "dfq_pool_batch", "dfq_server_create", "dfq_server_submit", "dfq_server_poll", "dfq_server_levels",
     "dfq_server_release", "dfq_server_pending", "dfq_server_destroy", "dfq_server_replay",
+    "dfq_set_host_threads", "dfq_host_threads",
 ]
 BATCH_GRAPH = 1
 
@@ -112,6 +113,9 @@ def lib() -> C.CDLL:
     L = C.CDLL(str(LIB_PATH))
     P32 = C.POINTER(C.c_int32)
     L.dfq_last_error.restype = C.c_char_p
+    L.dfq_set_host_threads.argtypes = [C.c_int32]
+    L.dfq_host_threads.argtypes = []
+    L.dfq_host_threads.restype = C.c_int32
     L.dfq_csr_load.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.POINTER(_Csr)]
     L.dfq_csr_save.argtypes = [C.c_char_p, C.POINTER(_Csr), C.c_int32]
     L.dfq_csr_from_edges.argtypes = [P32, P32, C.c_int64, C.c_int32, C.c_int32, C.POINTER(_Csr)]
@@ -236,6 +240,15 @@ class Csr:
         c = self._as_c()
         check(lib().dfq_pick_sources(C.byref(c), k, seed, _p32(out)))
         return out
+
+
+def set_host_threads(threads: int) -> None:
+    """Host threads for loaders, the CSR builder and generators (0 = default)."""
+    check(lib().dfq_set_host_threads(int(threads)))
+
+
+def host_threads() -> int:
+    return int(lib().dfq_host_threads())
 
 
 def load(path: str | os.PathLike, fmt: str = "auto", flags: int = 0) -> Csr:

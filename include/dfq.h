@@ -42,6 +42,13 @@ extern "C" {
 /* Message for the last failing call on this host thread ("" if none). */
 const char* dfq_last_error(void);
 
+/* Host threads used by the loaders, the CSR builder and the generators
+ * (0 = the DFQ_HOST_THREADS environment variable, else every hardware
+ * thread, at most 64).  Results never depend on it.  No reference
+ * counterpart: the reference's loader is one fscanf loop (DFQ:184-200). */
+int dfq_set_host_threads(int32_t threads);
+int32_t dfq_host_threads(void);
+
 /* ------------------------------------------------------------- host CSR */
 /*
  * Compressed sparse rows: offsets[n+1], cols[e].  Arrays are owned by the
@@ -74,7 +81,9 @@ typedef struct dfq_csr {
 /* Read a graph file.  Replaces the reference loader (DFQ:184-200) and adds the
  * SNAP edge list that the reference README documents (README.md:19-32) but no
  * reference binary reads.  SNAP edges are kept as given (directed) unless
- * flags ask otherwise; ids >= the header's N grow N to max id + 1. */
+ * flags ask otherwise; ids >= the header's N grow N to max id + 1.  Text is
+ * parsed by all host threads over line- or token-aligned pieces; the result
+ * and any error message are those of a serial reader. */
 int dfq_csr_load(const char* path, int32_t format, int32_t flags, dfq_csr* out);
 
 /* Write a graph as SNAP text, reference .dat text, or binary CSR. */

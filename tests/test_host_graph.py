@@ -137,3 +137,131 @@ def test_pick_sources():
     assert len(set(s.tolist())) == 64
     assert np.all(g.degrees()[s] > 0)
     assert np.array_equal(s, g.pick_sources(64, seed=4))
+
+
+# ---------------------------------------------------------------- parallel host I/O
+@pytest.fixture
+def host_threads():
+    yield d.set_host_threads
+    d.set_host_threads(0)
+
+
+@pytest.mark.parametrize("fmt", ["snap", "dat"])
+def test_parallel_text_io_matches_serial(tmp_path, fmt, host_threads):
+    """Text written and parsed over 2..13 pieces is byte- and CSR-identical to
+    the one-thread result, with and without builder flags."""
+    g = d.gen_rmat(11, 8, seed=5)
+    g.source = 7
+    host_threads(1)
+    g.save(tmp_path / "one", fmt)
+    ref = d.load(tmp_path / "one")
+    flags = d.CSR_SYMMETRIZE | d.CSR_DEDUP | d.CSR_NO_SELF_LOOPS
+    ref_f = d.load(tmp_path / "one", flags=flags)
+    one = (tmp_path / "one").read_bytes()
+    assert np.array_equal(ref.offsets, g.offsets) and np.array_equal(ref.cols, g.cols)
+    for t in (2, 3, 8, 13):
+        host_threads(t)
+        assert d.host_threads() == t
+        g.save(tmp_path / f"t{t}", fmt)
+        assert (tmp_path / f"t{t}").read_bytes() == one
+        h = d.load(tmp_path / f"t{t}")
+        assert np.array_equal(h.offsets, ref.offsets) and np.array_equal(h.cols, ref.cols)
+        assert h.source == (7 if fmt == "dat" else 0)
+        hf = d.load(tmp_path / f"t{t}", flags=flags)
+        assert np.array_equal(hf.offsets, ref_f.offsets) and np.array_equal(hf.cols, ref_f.cols)
+
+
+def test_parallel_csr_builder_is_stable(host_threads):
+    """The chunked counting sort keeps input order within each row (no DEDUP),
+    so every thread count gives the serial CSR."""
+    rng = np.random.default_rng(3)
+    m, n = 20000, 300
+    src = rng.integers(0, n, m, dtype=np.int32)
+    dst = rng.integers(0, n, m, dtype=np.int32)
+    for flags in (0, d.CSR_SYMMETRIZE, d.CSR_NO_SELF_LOOPS | d.CSR_SYMMETRIZE, d.CSR_DEDUP | d.CSR_SYMMETRIZE):
+        host_threads(1)
+        a = d.from_edges(src, dst, n, flags)
+        for t in (2, 5, 16):
+            host_threads(t)
+            b = d.from_edges(src, dst, n, flags)
+            assert np.array_equal(a.offsets, b.offsets) and np.array_equal(a.cols, b.cols), (flags, t)
+    # the serial definition: row u lists, in input order, v for every u->v
+    host_threads(7)
+    c = d.from_edges(src, dst, n)
+    for u in (0, 17, 299):
+        assert c.cols[c.offsets[u]:c.offsets[u + 1]].tolist() == dst[src == u].tolist()
+
+
+def _edge_lines(k):
+    return "".join(f"{i % 97}\t{(i * 7) % 101}\n" for i in range(k))
+
+
+@pytest.mark.parametrize("body,expect", [
+    (_edge_lines(300) + "12 x\n" + _edge_lines(400), "edge line 301 is not"),
+    (_edge_lines(700) + "5 4294967296\n" + _edge_lines(10), "edge line 701 has id out of int32 range"),
+    ("# c\n" + _edge_lines(50) + "# Nodes: 9 Edges: 1\n" + _edge_lines(50) + "7\n", "edge line 101 is not"),
+])
+def test_parallel_snap_errors_name_the_serial_line(tmp_path, body, expect, host_threads):
+    p = tmp_path / "bad.txt"
+    p.write_text("# Nodes: 200 Edges: 10\n" + body)
+    msgs = set()
+    for t in (1, 3, 11):
+        host_threads(t)
+        with pytest.raises(d.DfqError) as e:
+            d.load(p)
+        assert e.value.name == "EFORMAT" and expect in str(e.value)
+        msgs.add(str(e.value))
+    assert len(msgs) == 1
+
+
+def _dat(n, e, nodes, edges):
+    return f"{n} {e} 0\n" + "".join(f"{a} {b}\n" for a, b in nodes) + "".join(f"{a} {b}\n" for a, b in edges)
+
+
+@pytest.mark.parametrize("which,expect", [
+    ("node_malformed", "node record 50 missing or malformed"),
+    ("node_range", "node 100 has start=0 length=999999"),
+    ("edge_range", "edge 400 targets 5000 outside [0,200)"),
+    ("edge_malformed", "edge record 401 missing or malformed"),
+    ("truncated", "edge record 999 missing or malformed"),
+    ("truncated_nodes", "node record 150 missing or malformed"),
+])
+def test_parallel_dat_errors_name_the_serial_record(tmp_path, which, expect, host_threads):
+    n, e = 200, 1000
+    nodes = [(5 * i, 5) for i in range(n)]
+    edges = [((i * 13) % n, 1) for i in range(e)]
+    if which == "node_malformed":
+        nodes[50] = ("1z", 5)
+        nodes[120] = (0, 999999)  # a later error must not win
+    if which == "node_range":
+        nodes[100] = (0, 999999)
+        edges[3] = (5000, 1)
+    if which == "edge_range":
+        edges[400] = (5000, 1)
+        edges[700] = ("q", 1)
+    if which == "edge_malformed":
+        edges[401] = (3, "1.5")
+    text = _dat(n, e, nodes, edges)
+    if which == "truncated":
+        text = text[: text.rstrip("\n").rfind("\n") + 1]
+    if which == "truncated_nodes":
+        text = f"{n} {e} 0\n" + "".join(f"{a} {b}\n" for a, b in nodes[:150])
+    p = tmp_path / "bad.dat"
+    p.write_text(text)
+    msgs = set()
+    for t in (1, 4, 9):
+        host_threads(t)
+        with pytest.raises(d.DfqError) as ex:
+            d.load(p)
+        assert ex.value.name == "EFORMAT" and expect in str(ex.value), str(ex.value)
+        msgs.add(str(ex.value))
+    assert len(msgs) == 1
+
+
+def test_set_host_threads_bounds():
+    with pytest.raises(d.DfqError):
+        d.set_host_threads(-1)
+    with pytest.raises(d.DfqError):
+        d.set_host_threads(1000)
+    d.set_host_threads(0)
+    assert d.host_threads() >= 1
