@@ -43,9 +43,8 @@ struct dfq_graph {
     int bitmap_words = 0;
     int2* ovf[2] = {nullptr, nullptr};
     int32_t* ovfv[2] = {nullptr, nullptr};
-    int4* large[2] = {nullptr, nullptr};
-    int32_t* piece_owner[2] = {nullptr, nullptr};
-    int large_cap = 0;
+    int2* piece[2] = {nullptr, nullptr};
+    int32_t* piece_v[2] = {nullptr, nullptr};
     int piece_cap = 0;
     dfqk::Control* ctl = nullptr;
     dfqk::Control* ctl_host = nullptr;  // pinned copy for status / stats
@@ -151,8 +150,8 @@ void release(dfq_graph* g) {
     for (int i = 0; i < 2; ++i) {
         cudaFree(g->ovf[i]);
         cudaFree(g->ovfv[i]);
-        cudaFree(g->large[i]);
-        cudaFree(g->piece_owner[i]);
+        cudaFree(g->piece[i]);
+        cudaFree(g->piece_v[i]);
     }
     cudaFree(g->ctl);
     if (g->ctl_host) cudaFreeHost(g->ctl_host);
@@ -215,10 +214,9 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     for (int i = 0; i < 2; ++i) {
         p.ovf[i] = g->ovf[i];
         p.ovfv[i] = g->ovfv[i];
-        p.large[i] = g->large[i];
-        p.piece_owner[i] = g->piece_owner[i];
+        p.piece[i] = g->piece[i];
+        p.piece_v[i] = g->piece_v[i];
     }
-    p.large_cap = g->large_cap;
     p.piece_cap = g->piece_cap;
     p.ovf_cap = g->n;
     p.ctl = g->ctl;
@@ -340,13 +338,12 @@ int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int
     g->bitmap_words = (int)(((int64_t)n + 31) / 32);
     G_TRY(dev_alloc(&g->bitmap, ((size_t)g->bitmap_words + 31) & ~(size_t)31));
     G_TRY(dev_alloc(&g->levels_tmp, (size_t)n));
-    g->large_cap = (int)std::min<int64_t>((int64_t)n, e / kMinLargeDegree + 1) + 1;
-    g->piece_cap = (int)std::min<int64_t>((int64_t)1 << 30, e / kMinPiece + g->large_cap + 2);
+    g->piece_cap = dfqk::piece_capacity(n, e, kMinLargeDegree, kMinPiece);
     for (int i = 0; i < 2; ++i) {
         G_TRY(dev_alloc(&g->ovf[i], (size_t)n));
         G_TRY(dev_alloc(&g->ovfv[i], (size_t)n));
-        G_TRY(dev_alloc(&g->large[i], (size_t)g->large_cap));
-        G_TRY(dev_alloc(&g->piece_owner[i], (size_t)g->piece_cap));
+        G_TRY(dev_alloc(&g->piece[i], (size_t)g->piece_cap));
+        G_TRY(dev_alloc(&g->piece_v[i], (size_t)g->piece_cap));
     }
     G_TRY(dev_alloc(&g->ctl, 1));
     G_CUDA(cudaMallocHost((void**)&g->ctl_host, sizeof(dfqk::Control)));
@@ -445,6 +442,30 @@ int dfq_bfs_last_trace(dfq_graph* g, int64_t* start_ns, int32_t* frontier, int32
     for (int i = 0; i < n; ++i) {
         start_ns[i] = c.trace_ns[i];
         frontier[i] = c.trace_frontier[i];
+    }
+    return n;
+}
+
+int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels) {
+    clear_error();
+    if (!g || max_levels < 0 || (max_levels > 0 && !out))
+        return fail(DFQ_EINVAL, "dfq_bfs_last_levels: bad arguments");
+    DeviceGuard dg(g->device);
+    int rc = fill_stats(g, nullptr);
+    if (rc) return rc;
+    const dfqk::Control& c = *g->ctl_host;
+    int n = std::min(std::min(max_levels, dfqk::kTraceLevels), c.stats.levels + 1);
+    for (int i = 0; i < n; ++i) {
+        dfq_level_info& o = out[i];
+        memset(&o, 0, sizeof o);
+        o.start_ns = c.trace_ns[i];
+        o.frontier = c.trace_frontier[i];
+        o.edges = c.trace_edges[i];
+        o.overflow = c.trace_ovf[i];
+        o.pieces = c.trace_pieces[i];
+        o.probe = c.trace_probe[i];
+        o.last_done_ns = (int64_t)c.trace_done_last[i];
+        o.first_done_ns = c.trace_done_first[i] ? (int64_t)~c.trace_done_first[i] : 0;
     }
     return n;
 }

@@ -60,10 +60,9 @@ __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, i
     for (int i = 0; i < 2; ++i) {
         sp.ovf[i] = ws.ovf[i];
         sp.ovfv[i] = ws.ovfv[i];
-        sp.large[i] = ws.large[i];
-        sp.piece_owner[i] = ws.piece_owner[i];
+        sp.piece[i] = ws.piece[i];
+        sp.piece_v[i] = ws.piece_v[i];
     }
-    sp.large_cap = ws.large_cap;
     sp.piece_cap = ws.piece_cap;
     sp.ovf_cap = g.n;
     sp.ctl = bp.ctls + qi;
@@ -77,56 +76,57 @@ __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, i
     sp.timeout_ns = bp.timeout_ns;
 }
 
+// This block's narrow-query workspace.
+__device__ __forceinline__ Workspace block_workspace(const BatchParams& bp) {
+    Workspace bw;
+    unsigned char* base = bp.block_ws + bp.block_ws_stride * blockIdx.x;
+    const WsLayout& l = bp.block_lay;
+    bw.bitmap = (unsigned*)(base + l.bitmap);
+    for (int i = 0; i < 2; ++i) {
+        bw.ovf[i] = (int2*)(base + l.ovf[i]);
+        bw.ovfv[i] = (int*)(base + l.ovfv[i]);
+        bw.piece[i] = (int2*)(base + l.piece[i]);
+        bw.piece_v[i] = (int*)(base + l.piece_v[i]);
+    }
+    bw.piece_cap = l.piece_cap;
+    return bw;
+}
+
+// Wide queries first, one after another on the whole grid; then every block
+// pulls narrow queries and runs each alone.  One call site of bfs_run (the
+// group shape is chosen per query) keeps the kernel to one inlined copy.
 template <int B, bool PAR>
 __global__ void __launch_bounds__(B, 1024 / B) dfq_batch_kernel(const __grid_constant__ BatchParams bp) {
     __shared__ Params sp;
-    __shared__ int s_q;
+    __shared__ int s_q, s_gsize, s_grank;
     init_warp_barriers<B, PAR>(bp.local_cap, bp.piece_edges);
     WarpState ws{0u, false};
     if (blockIdx.x == 0 && threadIdx.x == 0) *bp.t0 = (long long)globaltimer();
-
-    // wide queries: the whole grid, one after another
-    for (int k = 0; k < bp.n_wide; ++k) {
-        const int qi = bp.wide_list[k];
+    for (int k = 0;; ++k) {
         if (threadIdx.x == 0) {
-            fill_params(sp, bp, qi, bp.wide_ws);
-            if (blockIdx.x == 0) bp.queries[qi].t_start = (long long)globaltimer();
-        }
-        __syncthreads();
-        bfs_run<B, PAR>(sp, (int)gridDim.x, (int)blockIdx.x, ws);
-        if (blockIdx.x == 0 && threadIdx.x == 0) bp.queries[qi].t_end = (long long)globaltimer();
-        __syncthreads();
-    }
-
-    // narrow queries: each block pulls one at a time and runs it alone
-    Workspace bw;
-    {
-        unsigned char* base = bp.block_ws + bp.block_ws_stride * blockIdx.x;
-        const WsLayout& l = bp.block_lay;
-        bw.bitmap = (unsigned*)(base + l.bitmap);
-        for (int i = 0; i < 2; ++i) {
-            bw.ovf[i] = (int2*)(base + l.ovf[i]);
-            bw.ovfv[i] = (int*)(base + l.ovfv[i]);
-            bw.large[i] = (int4*)(base + l.large[i]);
-            bw.piece_owner[i] = (int*)(base + l.owner[i]);
-        }
-        bw.large_cap = l.large_cap;
-        bw.piece_cap = l.piece_cap;
-    }
-    while (true) {
-        if (threadIdx.x == 0) {
-            const int k = atomicAdd(bp.narrow_next, 1);
-            s_q = k < bp.n_narrow ? bp.narrow_list[k] : -1;
-            if (s_q >= 0) {
-                fill_params(sp, bp, s_q, bw);
-                bp.queries[s_q].t_start = (long long)globaltimer();
+            if (k < bp.n_wide) {
+                s_q = bp.wide_list[k];
+                s_gsize = (int)gridDim.x;
+                s_grank = (int)blockIdx.x;
+                fill_params(sp, bp, s_q, bp.wide_ws);
+                if (blockIdx.x == 0) bp.queries[s_q].t_start = (long long)globaltimer();
+            } else {
+                const int j = atomicAdd(bp.narrow_next, 1);
+                s_q = j < bp.n_narrow ? bp.narrow_list[j] : -1;
+                s_gsize = 1;
+                s_grank = 0;
+                if (s_q >= 0) {
+                    fill_params(sp, bp, s_q, block_workspace(bp));
+                    bp.queries[s_q].t_start = (long long)globaltimer();
+                }
             }
         }
         __syncthreads();
         const int qi = s_q;
         if (qi < 0) break;
-        bfs_run<B, PAR>(sp, 1, 0, ws);
-        if (threadIdx.x == 0) bp.queries[qi].t_end = (long long)globaltimer();
+        const int gsize = s_gsize;
+        bfs_run<B, PAR>(sp, gsize, s_grank, ws);
+        if (threadIdx.x == 0 && (gsize == 1 || blockIdx.x == 0)) bp.queries[qi].t_end = (long long)globaltimer();
         __syncthreads();
     }
 }
@@ -358,10 +358,9 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     for (int i = 0; i < 2; ++i) {
         prm.ovf[i] = w.ovf[i];
         prm.ovfv[i] = w.ovfv[i];
-        prm.large[i] = w.large[i];
-        prm.piece_owner[i] = w.piece_owner[i];
+        prm.piece[i] = w.piece[i];
+        prm.piece_v[i] = w.piece_v[i];
     }
-    prm.large_cap = w.large_cap;
     prm.piece_cap = w.piece_cap;
     prm.ovf_cap = p->n[graph];
     prm.ctl = p->d_ctl1;

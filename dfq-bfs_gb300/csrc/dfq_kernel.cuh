@@ -85,6 +85,13 @@ struct Control {
     DevStats stats;
     long long trace_ns[kTraceLevels];   // %globaltimer when level L starts (block 0)
     int trace_frontier[kTraceLevels];   // frontier entries of level L
+    // per-level profile (first kTraceLevels levels)
+    int trace_edges[kTraceLevels];      // degree sum of level L's frontier (edges it scans)
+    int trace_ovf[kTraceLevels];        // of its entries, those in the global overflow queue
+    int trace_pieces[kTraceLevels];     // large-list pieces
+    int trace_probe[kTraceLevels];      // 1 if level L probed the bitmap before claiming
+    unsigned long long trace_done_last[kTraceLevels];   // latest block finish
+    unsigned long long trace_done_first[kTraceLevels];  // ~(earliest block finish), 0 = none
 };
 
 struct Params {
@@ -99,9 +106,8 @@ struct Params {
     int2* ovf[2];   // (start, degree) overflow entries, ovf_cap each
     int* ovfv[2];   // their vertex ids (parents only)
     int ovf_cap;    // n (a vertex is queued once per BFS) unless a bounded workspace says less
-    int4* large[2]; // (start, degree, first piece, vertex), capacity large_cap
-    int* piece_owner[2];  // piece -> large-queue slot, capacity piece_cap
-    int large_cap;
+    int2* piece[2];   // large-list pieces: edge range [lo, hi) of the list, piece_cap each
+    int* piece_v[2];  // the vertex each piece belongs to (parents only)
     int piece_cap;
     Control* ctl;
     int medium_min;
@@ -113,6 +119,19 @@ struct Params {
     int use_tma;
     long long timeout_ns;
 };
+
+// Pieces one level can produce with pieces of at least min_piece (>= 64)
+// edges and large lists of at least min_large edges: a list of degree d cut
+// from its aligned floor (at most 3 entries before it) makes fewer than
+// (d + 3) / piece + 1 pieces, a frontier's degrees sum to at most e, and at
+// most min(n, e / min_large) lists are large.
+__host__ __device__ inline int piece_capacity(long long n, long long e, int min_large, int min_piece) {
+    long long large = e / min_large + 1;
+    if (large > n) large = n;
+    large += 1;
+    const long long cap = e / min_piece + large + large / 16 + 2;
+    return (int)(cap < (1LL << 30) ? cap : (1LL << 30));
+}
 
 // ------------------------------------------------------------ PTX helpers
 __device__ __forceinline__ unsigned long long globaltimer() {
@@ -426,20 +445,63 @@ __device__ __forceinline__ void push_local(const Params& p, const Lv& lv, unsign
     }
 }
 
-__device__ __forceinline__ void push_large(const Params& p, const Lv& lv, int st, int dg, int v) {
-    const unsigned np = (unsigned)((dg + p.piece_edges - 1) / p.piece_edges);
-    unsigned long long old = atomicAdd(&p.ctl->lv[lv.cslot].large_pack, (1ull << 32) | np);
-    const int slot = (int)(old >> 32);
-    const unsigned poff = (unsigned)old;
-    atomicAdd(&sh.large_pushed, 1);
-    atomicAdd(&sh.large_edges, dg);
-    if (slot >= p.large_cap || poff + np > (unsigned)p.piece_cap) {
-        set_error(p.ctl, kErrQueueCap, slot, (int)poff);
-        return;
+// Push this warp's claimed large-degree vertices (bit j of lm: entry j of
+// this lane) with one atomic for the whole warp; slots and piece ranges are
+// handed out in lane order.  A list [st, st + dg) is cut at multiples of the
+// piece size counted from its 16-byte aligned floor a0 = st & ~3, so every
+// piece's staged span is at most piece_edges entries and starts aligned.
+// Warp-collective.
+__device__ __forceinline__ int pieces_of(int st, int dg, int P) { return (st + dg - (st & ~3) + P - 1) / P; }
+
+template <bool PAR>
+__device__ __forceinline__ void push_large(const Params& p, const Lv& lv, unsigned lm, const int (&st)[4],
+                                           const int (&dg)[4], const int (&v)[4]) {
+    const int lane = threadIdx.x & 31;
+    const int P = p.piece_edges;
+    int npl = 0;
+    unsigned dsum = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (lm >> j & 1) {
+            npl += pieces_of(st[j], dg[j], P);
+            dsum += (unsigned)dg[j];
+        }
+    int incl = npl;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int tt = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += tt;
     }
-    (lv.out ? p.large[1] : p.large[0])[slot] = make_int4(st, dg, (int)poff, v);
-    int* owner = lv.out ? p.piece_owner[1] : p.piece_owner[0];
-    for (unsigned i = 0; i < np; ++i) owner[poff + i] = slot;
+    const unsigned totp = (unsigned)__shfl_sync(kFull, incl, 31);
+    const unsigned totc = __reduce_add_sync(kFull, (unsigned)__popc(lm));
+    const unsigned totd = __reduce_add_sync(kFull, dsum);
+    unsigned base = 0;
+    if (lane == 0) {
+        const unsigned long long old =
+            atomicAdd(&p.ctl->lv[lv.cslot].large_pack, ((unsigned long long)totc << 32) | totp);
+        base = (unsigned)old;
+        atomicAdd(&sh.large_pushed, (int)totc);
+        atomicAdd(&sh.large_edges, (int)totd);
+        if (base + totp > (unsigned)p.piece_cap) set_error(p.ctl, kErrQueueCap, (int)base, (int)totp);
+    }
+    base = __shfl_sync(kFull, base, 0);
+    if (!lm) return;
+    // pieces past the capacity are dropped (the error is recorded above);
+    // readers clamp the piece count to the capacity, so every piece read
+    // was written at this level
+    unsigned poff = base + (unsigned)(incl - npl);
+    int2* pc = lv.out ? p.piece[1] : p.piece[0];
+    int* pv = lv.out ? p.piece_v[1] : p.piece_v[0];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (!(lm >> j & 1)) continue;
+        const int a0 = st[j] & ~3, e1 = st[j] + dg[j], np = pieces_of(st[j], dg[j], P);
+        for (int i = 0; i < np && poff + (unsigned)i < (unsigned)p.piece_cap; ++i) {
+            pc[poff + i] = make_int2(max(st[j], a0 + i * P), min(e1, a0 + (i + 1) * P));
+            if (PAR) pv[poff + i] = v[j];
+        }
+        poff += (unsigned)np;
+    }
 }
 
 // Scan up to four neighbours per lane: probe, claim, record, push.
@@ -503,16 +565,18 @@ __device__ __forceinline__ void visit4(const Params& p, const Lv& lv, Tally& t, 
             }
         }
     }
+    unsigned lm = 0;
     if (claim) {
         t.claims += __popc(claim);
         sh.claimed = 1;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             if (!(claim >> j & 1) || dg[j] == 0) continue;
-            if (dg[j] >= p.large_min) push_large(p, lv, st[j], dg[j], v[j]);
+            if (dg[j] >= p.large_min) lm |= 1u << j;
             else loc |= 1u << j;
         }
     }
+    if (__any_sync(kFull, lm)) push_large<PAR>(p, lv, lm, st, dg, v);
     push_local<PAR>(p, lv, loc, st, dg, v);
 }
 
@@ -521,23 +585,29 @@ __device__ __forceinline__ void visit4(const Params& p, const Lv& lv, Tally& t, 
 template <bool PAR>
 __device__ __forceinline__ void claim1(const Params& p, const Lv& lv, Tally& t, bool has, int v, int par) {
     bool won = false;
+    int so = 0, eo = 0;
     if (has) {
+        // row bounds fetched alongside the claim: a candidate that passed the
+        // probe is usually still unvisited, so these loads are rarely wasted
+        so = __ldg(p.offsets + v);
+        eo = __ldg(p.offsets + v + 1);
         const unsigned bit = 1u << (v & 31);
         won = !(atomicOr(&p.bitmap[v >> 5], bit) & bit);
     }
     int st[4] = {0, 0, 0, 0}, dg[4] = {0, 0, 0, 0};
     const int vv[4] = {v, 0, 0, 0};
-    unsigned loc = 0;
+    unsigned loc = 0, lm = 0;
     if (won) {
         p.levels[v] = lv.next;
         if (PAR) p.parents[v] = par;
-        st[0] = __ldg(p.offsets + v);
-        dg[0] = __ldg(p.offsets + v + 1) - st[0];
+        st[0] = so;
+        dg[0] = eo - so;
         t.claims += 1;
         sh.claimed = 1;
-        if (dg[0] >= p.large_min) push_large(p, lv, st[0], dg[0], v);
+        if (dg[0] >= p.large_min) lm = 1;
         else if (dg[0] > 0) loc = 1;
     }
+    if (__any_sync(kFull, lm)) push_large<PAR>(p, lv, lm, st, dg, vv);
     push_local<PAR>(p, lv, loc, st, dg, vv);
 }
 
@@ -601,6 +671,73 @@ __device__ __forceinline__ void probe4(const Params& p, const Lv& lv, Tally& t, 
     __syncwarp();
     r.n += tot;
     ring_drain<PAR>(p, lv, t, r, false);
+}
+
+// Probe levels, eight neighbours per lane (all of one vertex, par0): the
+// eight bitmap loads are in flight together; candidates are appended in two
+// halves of at most 128 with a drain between, so the ring (< 32 entries
+// between calls) never holds more than 159.  One scan serves both halves
+// (counts packed in 16-bit fields).  Warp-collective.
+template <bool PAR>
+__device__ __forceinline__ void probe8(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[8],
+                                       unsigned vm, int par0) {
+    const int lane = threadIdx.x & 31;
+    unsigned w[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) w[j] = (vm >> j & 1) ? p.bitmap[v[j] >> 5] : 0xffffffffu;
+    unsigned cm = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if ((vm >> j & 1) && !((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
+    t.edges += __popc(vm);
+    if (!__any_sync(kFull, cm)) return;
+    const int c_lo = __popc(cm & 15u), c_hi = __popc(cm >> 4);
+    int incl = c_lo | (c_hi << 16);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int tt = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += tt;
+    }
+    const int tot = __shfl_sync(kFull, incl, 31);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int th = h ? (tot >> 16) : (tot & 0xffff);
+        if (th == 0) continue;
+        int pos = r.head + r.n + (h ? (incl >> 16) - c_hi : (incl & 0xffff) - c_lo);
+#pragma unroll
+        for (int j = 4 * h; j < 4 * h + 4; ++j) {
+            if (cm >> j & 1) {
+                const int idx = pos & (kRing - 1);
+                r.v[idx] = v[j];
+                if (PAR) r.v[kRing + idx] = par0;
+                ++pos;
+            }
+        }
+        __syncwarp();
+        r.n += th;
+        ring_drain<PAR>(p, lv, t, r, false);
+    }
+}
+
+// Expand one staged piece on a probe level: buf holds entries [0, tw) of the
+// piece's aligned span, the piece itself is [off, tw); lanes take eight
+// consecutive entries (two 16-byte shared-memory reads).  Warp-collective.
+template <bool PAR>
+__device__ __forceinline__ void probe_piece(const Params& p, const Lv& lv, Tally& t, Ring& r, const int* buf,
+                                            int off, int tw, int par0) {
+    const int lane = threadIdx.x & 31;
+    for (int base = 0; base < tw; base += 256) {
+        const int w8 = base + 8 * lane;
+        int4 x0 = make_int4(0, 0, 0, 0), x1 = x0;
+        if (w8 < tw) x0 = *reinterpret_cast<const int4*>(buf + w8);
+        if (w8 + 4 < tw) x1 = *reinterpret_cast<const int4*>(buf + w8 + 4);
+        const int v[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+        unsigned vm = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (w8 + j >= off && w8 + j < tw) vm |= 1u << j;
+        probe8<PAR>(p, lv, t, r, v, vm, par0);
+    }
 }
 
 // Probe or claim-at-once, by level.  Warp-collective.
@@ -736,10 +873,17 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             const int s0 = p.offsets[src], d = p.offsets[src + 1] - s0;
             if (d > 0) {
                 if (d >= p.large_min) {
-                    const int np = (d + P - 1) / P;
-                    p.large[0][0] = make_int4(s0, d, 0, src);
-                    for (int i = 0; i < np; ++i) p.piece_owner[0][i] = 0;
-                    ctl->lv[0].large_pack = (1ull << 32) | (unsigned)np;
+                    // the source's list in pieces, cut as push_large cuts lists
+                    const int a0 = s0 & ~3, np = (s0 + d - a0 + P - 1) / P;
+                    if (np <= p.piece_cap) {
+                        for (int i = 0; i < np; ++i) {
+                            p.piece[0][i] = make_int2(max(s0, a0 + i * P), min(s0 + d, a0 + (i + 1) * P));
+                            if (PAR) p.piece_v[0][i] = src;
+                        }
+                        ctl->lv[0].large_pack = (1ull << 32) | (unsigned)np;
+                    } else {
+                        set_error(ctl, kErrQueueCap, np, p.piece_cap);
+                    }
                 } else {
                     p.ovf[0][0] = make_int2(s0, d);
                     if (PAR) p.ovfv[0][0] = src;
@@ -784,8 +928,10 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             cz->large_pack = 0ull;
         }
         const int in = L & 1;
-        const int n_ovf = sh.in[1];
-        const int total_pieces = sh.in[3];
+        // counts past a queue's capacity (recorded as an error when pushed)
+        // are clamped so only entries written at this level are read
+        const int n_ovf = min(sh.in[1], p.ovf_cap);
+        const int total_pieces = min(sh.in[3], p.piece_cap);
         Lv lv;
         lv.next = L + 1;
         lv.out = in ^ 1;
@@ -802,6 +948,12 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         // where it scans fewer edges than one 4-edge round per lane of the
         // grid; 2 = decide per level
         lv.probe = p.probe_first == 2 ? (sh.in[4] >= 128 * nwarps ? 1 : 0) : p.probe_first;
+        if (grank == 0 && tid == 0 && L < kTraceLevels) {
+            ctl->trace_edges[L] = sh.in[4];
+            ctl->trace_ovf[L] = n_ovf;
+            ctl->trace_pieces[L] = total_pieces;
+            ctl->trace_probe[L] = lv.probe;
+        }
 
         // (1) this block's own queue from the previous level, 32 entries per grab
         {
@@ -825,52 +977,68 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         //     otherwise the first 3/4 go round-robin and the rest are pulled
         //     from a counter
         if (total_pieces > 0 && !warp_failed) {
-            const int4* large_in = p.large[in];
-            const int* owner_in = p.piece_owner[in];
+            const int2* pin = p.piece[in];
+            const int* pvin = p.piece_v[in];
             const int p_static = total_pieces <= nwarps ? total_pieces : total_pieces - total_pieces / 4;
-            int s_next = gwarp;
-            int m_e0 = 0, m_cnt = -1, m_off = 0, m_par = 0;  // lane 0: next piece
-            auto fetch = [&](int b) {  // lane 0 only
-                int g;
-                if (s_next < p_static) { g = s_next; s_next += nwarps; }
-                else if (p_static < total_pieces) g = p_static + atomicAdd(&cin->large_grab, 1);
-                else g = total_pieces;
-                if (g >= total_pieces) { m_cnt = -1; return; }
-                const int slot = __ldcg(owner_in + g);
-                const int4 ent = __ldcg(large_in + slot);
-                const int e0 = ent.x + (g - ent.z) * P;
-                const int e1 = min(e0 + P, ent.x + ent.y);
-                const int a0 = e0 & ~3, a1 = (e1 + 3) & ~3;
-                m_e0 = e0;
-                m_cnt = e1 - e0;
-                m_off = e0 - a0;
-                m_par = ent.w;
-                if (p.use_tma) {
-                    int* dst = wbuf0 + b * (P + 16);
-                    const unsigned bytes = (unsigned)(a1 - a0) * 4u;
-                    mbar_arrive_expect_tx(&wbar[b], bytes);
-                    tma_load_1d(dst, p.cols + a0, bytes, &wbar[b]);
+            // lane 0 runs a pipeline one piece deep in each stage: while piece
+            // k is expanded, piece k+1's copy is in flight, piece k+2's range
+            // is being loaded and piece k+3's index has been taken, so no
+            // dependent load or atomic sits between two pieces.  The next
+            // static index lives in the warp's gather scratch (unused while
+            // pieces are expanded).
+            int* pq = wl;
+            auto grab = [&]() -> int {  // lane 0: next piece index (total_pieces: none)
+                const int sn = pq[0];
+                if (sn < p_static) { pq[0] = sn + nwarps; return sn; }
+                if (p_static < total_pieces) return p_static + atomicAdd(&cin->large_grab, 1);
+                return total_pieces;
+            };
+            auto desc = [&](int g, int2& d, int& u) {  // lane 0: piece g's range (empty: none)
+                d = make_int2(0, 0);
+                u = 0;
+                if (g < total_pieces) {
+                    d = __ldcg(pin + g);
+                    if (PAR) u = __ldcg(pvin + g);
                 }
             };
-            if (lane == 0) fetch(0);
+            auto issue = [&](const int2& d, int b) {  // lane 0: stage piece d into buffer b
+                if (p.use_tma && d.y > d.x) {
+                    const int a0 = d.x & ~3, a1 = (d.y + 3) & ~3;
+                    const unsigned bytes = (unsigned)(a1 - a0) * 4u;
+                    mbar_arrive_expect_tx(&wbar[b], bytes);
+                    tma_load_1d(wbuf0 + b * (P + 16), p.cols + a0, bytes, &wbar[b]);
+                }
+            };
+            int2 dc = make_int2(0, 0), dn = dc;
+            int uc = 0, un = 0, gn = total_pieces;
+            if (lane == 0) {
+                pq[0] = gwarp;
+                desc(grab(), dc, uc);
+                issue(dc, 0);
+                desc(grab(), dn, un);
+                gn = grab();
+            }
             int cb = 0;
             while (true) {
-                const int cnt = __shfl_sync(kFull, m_cnt, 0);
-                if (cnt < 0) break;
-                const int e0 = __shfl_sync(kFull, m_e0, 0);
-                const int off = __shfl_sync(kFull, m_off, 0);
-                const int par0 = __shfl_sync(kFull, m_par, 0);
-                if (lane == 0) fetch(cb ^ 1);
-                const int par[4] = {par0, par0, par0, par0};
+                const int lo = __shfl_sync(kFull, dc.x, 0), hi = __shfl_sync(kFull, dc.y, 0);
+                if (hi <= lo) break;
+                const int par0 = PAR ? __shfl_sync(kFull, uc, 0) : 0;
+                if (lane == 0) {
+                    issue(dn, cb ^ 1);
+                    dc = dn;
+                    uc = un;
+                    desc(gn, dn, un);
+                    gn = grab();
+                }
                 if (p.use_tma) {
                     const bool landed = mbar_wait_bounded(&wbar[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
                     if (__any_sync(kFull, !landed)) {
                         // never expand a buffer whose copy did not land: record the
                         // error, give this warp's copies one more bounded wait, stop
                         if (lane == 0) {
-                            set_error(ctl, kErrTmaTimeout, (int)blockIdx.x, e0);
+                            set_error(ctl, kErrTmaTimeout, (int)blockIdx.x, lo);
                             mbar_wait_bounded(&wbar[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
-                            if (m_cnt >= 0)
+                            if (dc.y > dc.x)
                                 mbar_wait_bounded(&wbar[cb ^ 1], (phase_bits >> (cb ^ 1)) & 1u, p.timeout_ns);
                         }
                         warp_failed = true;
@@ -878,22 +1046,27 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                     }
                     phase_bits ^= 1u << cb;
                     const int* buf = wbuf0 + cb * (P + 16);
-                    const int tw = off + cnt;
-                    for (int base = 0; base < tw; base += 128) {
-                        const int w4 = base + 4 * lane;
-                        int4 x = make_int4(0, 0, 0, 0);
-                        unsigned vm = 0;
-                        if (w4 < tw) {
-                            x = *reinterpret_cast<const int4*>(buf + w4);
+                    const int a0 = lo & ~3, off = lo - a0, tw = hi - a0;
+                    if (lv.probe) {
+                        probe_piece<PAR>(p, lv, t, ring, buf, off, tw, par0);
+                    } else {
+                        const int par[4] = {par0, par0, par0, par0};
+                        for (int base = 0; base < tw; base += 128) {
+                            const int w4 = base + 4 * lane;
+                            int4 x = make_int4(0, 0, 0, 0);
+                            unsigned vm = 0;
+                            if (w4 < tw) {
+                                x = *reinterpret_cast<const int4*>(buf + w4);
 #pragma unroll
-                            for (int j = 0; j < 4; ++j)
-                                if (w4 + j >= off && w4 + j < tw) vm |= 1u << j;
+                                for (int j = 0; j < 4; ++j)
+                                    if (w4 + j >= off && w4 + j < tw) vm |= 1u << j;
+                            }
+                            const int v[4] = {x.x, x.y, x.z, x.w};
+                            scan4<PAR>(p, lv, t, ring, v, vm, par);
                         }
-                        const int v[4] = {x.x, x.y, x.z, x.w};
-                        scan4<PAR>(p, lv, t, ring, v, vm, par);
                     }
                 } else {
-                    warp_expand<PAR>(p, lv, t, ring, e0, cnt, par0);
+                    warp_expand<PAR>(p, lv, t, ring, lo, hi - lo, par0);
                 }
                 __syncwarp();
                 cb ^= 1;
@@ -937,7 +1110,9 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
 
         // end of level: publish how much this block pushed, keep its queue
         __syncthreads();
+        unsigned long long done_ns = 0;  // when this block finished the level (thread 0)
         if (tid == 0) {
+            done_ns = globaltimer();
             const int kept = (int)(sh.local_pack >> 32);
             const int tot = kept + sh.ovf_pushed + sh.large_pushed;
             if (tot) {
@@ -956,6 +1131,11 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         }
         cur ^= 1;
         ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in);
+        if (tid == 0 && L < kTraceLevels) {
+            // recorded after the barrier: its release would otherwise wait for them
+            atomicMax(&ctl->trace_done_last[L], done_ns);
+            atomicMax(&ctl->trace_done_first[L], ~done_ns);
+        }
     }
 
     // ---- statistics

@@ -55,24 +55,23 @@ DeviceSetup g_setup[kMaxDevices];
 
 // Byte layout of the scratch array for one graph (256-byte aligned pieces).
 struct ScratchLayout {
-    size_t ctl, bitmap, ovf[2], ovfv[2], large[2], owner[2], total;
-    int bitmap_words, large_cap, piece_cap;
+    size_t ctl, bitmap, ovf[2], ovfv[2], piece[2], piece_v[2], total;
+    int bitmap_words, piece_cap;
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-ScratchLayout scratch_layout(int32_t n, int64_t e, const dfq_opts& o) {
+ScratchLayout scratch_layout(int32_t n, int64_t e, const dfq_opts& o, bool par) {
     ScratchLayout s;
     size_t p = 0;
     s.ctl = p;            p = align256(p + sizeof(dfqk::Control));
     s.bitmap_words = (int)(((int64_t)n + 31) / 32);
     s.bitmap = p;         p = align256(p + 4 * (((size_t)s.bitmap_words + 31) & ~(size_t)31));
-    s.large_cap = (int)std::min<int64_t>((int64_t)n, e / o.large_min_degree + 1) + 1;
-    s.piece_cap = (int)(e / o.piece_edges + s.large_cap + 2);
+    s.piece_cap = dfqk::piece_capacity(n, e, o.large_min_degree, o.piece_edges);
     for (int i = 0; i < 2; ++i) { s.ovf[i] = p;   p = align256(p + 8 * (size_t)n); }
     for (int i = 0; i < 2; ++i) { s.ovfv[i] = p;  p = align256(p + 4 * (size_t)n); }
-    for (int i = 0; i < 2; ++i) { s.large[i] = p; p = align256(p + 16 * (size_t)s.large_cap); }
-    for (int i = 0; i < 2; ++i) { s.owner[i] = p; p = align256(p + 4 * (size_t)s.piece_cap); }
+    for (int i = 0; i < 2; ++i) { s.piece[i] = p;   p = align256(p + 8 * (size_t)s.piece_cap); }
+    for (int i = 0; i < 2; ++i) { s.piece_v[i] = p; p = align256(p + (par ? 4 * (size_t)s.piece_cap : 256)); }
     s.total = p;
     return s;
 }
@@ -136,7 +135,7 @@ extern "C" int dfq_bfs_noalloc(const int32_t* offsets, const int32_t* cols, int3
         return fail(DFQ_EINVAL, "dfq_bfs_noalloc: cols must be 16-byte aligned and offsets/levels/parents 4-byte aligned");
     dfq_opts o;
     dfq_opts_default(&o);
-    const ScratchLayout sl = scratch_layout(n, e, o);
+    const ScratchLayout sl = scratch_layout(n, e, o, parents != nullptr);
     if (sl.total > (size_t)DFQ_NOALLOC_SCRATCH_BYTES)
         return fail(DFQ_ENOMEM, "dfq_bfs_noalloc: a graph with n=%d, e=%lld needs %zu bytes of scratch; the fixed "
                     "scratch array holds %zu (24 bytes per vertex + 0.2 per edge); use dfq_graph_create for larger graphs",
@@ -176,10 +175,9 @@ extern "C" int dfq_bfs_noalloc(const int32_t* offsets, const int32_t* cols, int3
     for (int i = 0; i < 2; ++i) {
         p.ovf[i] = (int2*)(base + sl.ovf[i]);
         p.ovfv[i] = (int*)(base + sl.ovfv[i]);
-        p.large[i] = (int4*)(base + sl.large[i]);
-        p.piece_owner[i] = (int*)(base + sl.owner[i]);
+        p.piece[i] = (int2*)(base + sl.piece[i]);
+        p.piece_v[i] = (int*)(base + sl.piece_v[i]);
     }
-    p.large_cap = sl.large_cap;
     p.piece_cap = sl.piece_cap;
     p.ovf_cap = n;
     p.ctl = ctl;

@@ -35,16 +35,15 @@ struct Workspace {
     unsigned* bitmap;
     int2* ovf[2];
     int* ovfv[2];
-    int4* large[2];
-    int* piece_owner[2];
-    int large_cap;
+    int2* piece[2];
+    int* piece_v[2];
     int piece_cap;
 };
 
 // Byte layout of one workspace for graphs up to n vertices and e edges.
 struct WsLayout {
-    size_t bitmap, ovf[2], ovfv[2], large[2], owner[2], total;
-    int large_cap, piece_cap;
+    size_t bitmap, ovf[2], ovfv[2], piece[2], piece_v[2], total;
+    int piece_cap;
 };
 
 inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -52,12 +51,11 @@ inline WsLayout ws_layout(long long n, long long e, int min_large, int min_piece
     WsLayout w;
     size_t o = 0;
     w.bitmap = o;  o = al256(o + 4 * (size_t)(((n + 31) / 32 + 31) & ~31LL));
-    w.large_cap = (int)std::min<long long>(n, e / min_large + 1) + 1;
-    w.piece_cap = (int)std::min<long long>(1LL << 30, e / min_piece + w.large_cap + 2);
+    w.piece_cap = piece_capacity(n, e, min_large, min_piece);
     for (int i = 0; i < 2; ++i) { w.ovf[i] = o;   o = al256(o + 8 * (size_t)std::max<long long>(n, 1)); }
     for (int i = 0; i < 2; ++i) { w.ovfv[i] = o;  o = al256(o + (par ? 4 * (size_t)std::max<long long>(n, 1) : 256)); }
-    for (int i = 0; i < 2; ++i) { w.large[i] = o; o = al256(o + 16 * (size_t)w.large_cap); }
-    for (int i = 0; i < 2; ++i) { w.owner[i] = o; o = al256(o + 4 * (size_t)w.piece_cap); }
+    for (int i = 0; i < 2; ++i) { w.piece[i] = o;   o = al256(o + 8 * (size_t)w.piece_cap); }
+    for (int i = 0; i < 2; ++i) { w.piece_v[i] = o; o = al256(o + (par ? 4 * (size_t)w.piece_cap : 256)); }
     w.total = o;
     return w;
 }
@@ -166,10 +164,9 @@ inline Workspace ws_from(unsigned char* base, const WsLayout& l) {
     for (int i = 0; i < 2; ++i) {
         w.ovf[i] = (int2*)(base + l.ovf[i]);
         w.ovfv[i] = (int*)(base + l.ovfv[i]);
-        w.large[i] = (int4*)(base + l.large[i]);
-        w.piece_owner[i] = (int*)(base + l.owner[i]);
+        w.piece[i] = (int2*)(base + l.piece[i]);
+        w.piece_v[i] = (int*)(base + l.piece_v[i]);
     }
-    w.large_cap = l.large_cap;
     w.piece_cap = l.piece_cap;
     return w;
 }

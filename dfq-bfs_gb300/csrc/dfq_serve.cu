@@ -124,11 +124,10 @@ __device__ __forceinline__ void serve_params(Params& sp, const ServeParams& s, c
     for (int i = 0; i < 2; ++i) {
         sp.ovf[i] = ws.ovf[i];
         sp.ovfv[i] = ws.ovfv[i];
-        sp.large[i] = ws.large[i];
-        sp.piece_owner[i] = ws.piece_owner[i];
+        sp.piece[i] = ws.piece[i];
+        sp.piece_v[i] = ws.piece_v[i];
     }
     sp.ovf_cap = min(ovf_cap, g.n);
-    sp.large_cap = ws.large_cap;
     sp.piece_cap = ws.piece_cap;
     sp.ctl = ctl;
     sp.medium_min = s.medium_min;
@@ -206,6 +205,21 @@ __device__ __forceinline__ int form_gang(const ServeParams& s, unsigned long lon
     return m;
 }
 
+// This block's narrow-request workspace.
+__device__ __forceinline__ Workspace block_workspace(const ServeParams& s) {
+    Workspace bw;
+    unsigned char* base = s.block_ws + s.block_ws_stride * blockIdx.x;
+    bw.bitmap = (unsigned*)(base + s.block_lay.bitmap);
+    for (int i = 0; i < 2; ++i) {
+        bw.ovf[i] = (int2*)(base + s.block_lay.ovf[i]);
+        bw.ovfv[i] = (int*)(base + s.block_lay.ovfv[i]);
+        bw.piece[i] = (int2*)(base + s.block_lay.piece[i]);
+        bw.piece_v[i] = (int*)(base + s.block_lay.piece_v[i]);
+    }
+    bw.piece_cap = s.block_lay.piece_cap;
+    return bw;
+}
+
 template <int B, bool PAR>
 __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_constant__ ServeParams s) {
     __shared__ Params sp;
@@ -219,19 +233,6 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_con
     ServeDev* dev = s.dev;
     const unsigned mask = (unsigned)s.cap - 1;
 
-    Workspace bw;
-    {
-        unsigned char* base = s.block_ws + s.block_ws_stride * blockIdx.x;
-        bw.bitmap = (unsigned*)(base + s.block_lay.bitmap);
-        for (int i = 0; i < 2; ++i) {
-            bw.ovf[i] = (int2*)(base + s.block_lay.ovf[i]);
-            bw.ovfv[i] = (int*)(base + s.block_lay.ovfv[i]);
-            bw.large[i] = (int4*)(base + s.block_lay.large[i]);
-            bw.piece_owner[i] = (int*)(base + s.block_lay.owner[i]);
-        }
-        bw.large_cap = s.block_lay.large_cap;
-        bw.piece_cap = s.block_lay.piece_cap;
-    }
     if (tid == 0) s_next_gang = *(volatile unsigned long long*)&dev->gang_done;
     __syncthreads();
 
@@ -340,12 +341,18 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_con
         }
         const unsigned long long k = (unsigned long long)s_k;
         const unsigned slot = (unsigned)k & mask;
-        if (act == kActGang) {
-            if (tid == 0) serve_params(sp, s, s_req, s.wide_ws, s.wide_ovf_cap, &s.ctls[1][slot]);
-            __syncthreads();
-            const long long t0 = (long long)globaltimer();
-            bfs_run<B, PAR>(sp, s_size, s_rank, ws);
-            if (tid == 0) {
+        // one call site of bfs_run for both shapes keeps one inlined copy
+        const bool gang = act == kActGang;
+        if (!gang) zero_ctl(&s.ctls[0][slot], tid, B);
+        if (tid == 0) {
+            if (gang) serve_params(sp, s, s_req, s.wide_ws, s.wide_ovf_cap, &s.ctls[1][slot]);
+            else serve_params(sp, s, s_req, block_workspace(s), s.block_ovf_cap, &s.ctls[0][slot]);
+        }
+        __syncthreads();
+        const long long t0 = (long long)globaltimer();
+        bfs_run<B, PAR>(sp, gang ? s_size : 1, gang ? s_rank : 0, ws);
+        if (tid == 0) {
+            if (gang) {
                 s_next_gang = k + 1;
                 // a member's statistics are in once it counts itself out
                 __threadfence();
@@ -359,14 +366,7 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_serve_kernel(const __grid_con
                     *(volatile unsigned long long*)&dev->gang_done = k + 1;
                     __threadfence();
                 }
-            }
-        } else {  // narrow, alone
-            zero_ctl(&s.ctls[0][slot], tid, B);
-            if (tid == 0) serve_params(sp, s, s_req, bw, s.block_ovf_cap, &s.ctls[0][slot]);
-            __syncthreads();
-            const long long t0 = (long long)globaltimer();
-            bfs_run<B, PAR>(sp, 1, 0, ws);
-            if (tid == 0) {
+            } else {
                 publish_done(&s.done[0][slot], k, &s.ctls[0][slot], t0, (long long)globaltimer());
                 atomicSub(&dev->narrow_active, 1);
             }
@@ -655,16 +655,15 @@ int dfq_server_create(dfq_pool* pool, const dfq_server_opts* opts, dfq_server** 
     const long long qcap = std::min<long long>(nmax, o.narrow_queue_cap);
     WsLayout l = ws_layout(nmax, 0, kMinLarge, kMinPiece, par);
     {
-        // queues for qcap entries, large bin for at most 1 << 16 vertices
+        // queues for qcap entries, at most 1 << 18 large-list pieces per level
         size_t off = 0;
         l.bitmap = off;
         off = al256(off + 4 * (size_t)(((nmax + 31) / 32 + 31) & ~31LL));
         for (int i = 0; i < 2; ++i) { l.ovf[i] = off; off = al256(off + 8 * (size_t)qcap); }
         for (int i = 0; i < 2; ++i) { l.ovfv[i] = off; off = al256(off + (par ? 4 * (size_t)qcap : 256)); }
-        l.large_cap = 1 << 16;
         l.piece_cap = 1 << 18;
-        for (int i = 0; i < 2; ++i) { l.large[i] = off; off = al256(off + 16 * (size_t)l.large_cap); }
-        for (int i = 0; i < 2; ++i) { l.owner[i] = off; off = al256(off + 4 * (size_t)l.piece_cap); }
+        for (int i = 0; i < 2; ++i) { l.piece[i] = off; off = al256(off + 8 * (size_t)l.piece_cap); }
+        for (int i = 0; i < 2; ++i) { l.piece_v[i] = off; off = al256(off + (par ? 4 * (size_t)l.piece_cap : 256)); }
         l.total = off;
     }
     s->block_lay = l;

@@ -41,7 +41,7 @@ EXPORTS = [
     "dfq_pool_create", "dfq_pool_destroy", "dfq_pool_num_graphs", "dfq_pool_graph_info", "dfq_pool_bfs",
     "dfq_pool_batch", "dfq_server_create", "dfq_server_submit", "dfq_server_poll", "dfq_server_levels",
     "dfq_server_release", "dfq_server_pending", "dfq_server_destroy", "dfq_server_replay",
-    "dfq_set_host_threads", "dfq_host_threads",
+    "dfq_set_host_threads", "dfq_host_threads", "dfq_bfs_last_levels",
 ]
 BATCH_GRAPH = 1
 
@@ -89,6 +89,12 @@ class ServerResult(C.Structure):
     _fields_ = [("id", C.c_int64), ("tag", C.c_int64), ("status", C.c_int32), ("wide", C.c_int32),
                 ("depth", C.c_int32), ("retried", C.c_int32), ("reached", C.c_int64), ("edges", C.c_int64),
                 ("submit_us", C.c_double), ("done_us", C.c_double), ("device_us", C.c_double)]
+
+
+class LevelInfo(C.Structure):
+    _fields_ = [("start_ns", C.c_int64), ("first_done_ns", C.c_int64), ("last_done_ns", C.c_int64),
+                ("frontier", C.c_int32), ("edges", C.c_int32), ("overflow", C.c_int32),
+                ("pieces", C.c_int32), ("probe", C.c_int32), ("pad", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -174,6 +180,7 @@ def lib() -> C.CDLL:
         getattr(L, name).restype = C.c_int
     L.dfq_bfs_last_trace.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int32]
     L.dfq_bfs_last_trace.restype = C.c_int
+    L.dfq_bfs_last_levels.argtypes = [C.c_void_p, C.POINTER(LevelInfo), C.c_int32]
     L.dfq_bfs_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int64, C.c_int32, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.POINTER(Stats)]
     for name in ("dfq_csr_load", "dfq_csr_save", "dfq_csr_from_edges", "dfq_gen_zipf_geometric",
@@ -391,6 +398,29 @@ class Graph:
         if k < 0:
             check(k)
         return ns[:k], fr[:k]
+
+    def last_levels(self, max_levels: int = 64) -> list[dict]:
+        """Per-level profile of the last launch: frontier, edges scanned,
+        overflow entries, pieces, probe flag, and the level's time split into
+        work until the last block finished (us_work), the spread of block
+        finish times (us_spread) and the barrier until the next level began
+        (us_barrier; absent for the final level)."""
+        buf = (LevelInfo * max_levels)()
+        k = lib().dfq_bfs_last_levels(self.h, buf, max_levels)
+        if k < 0:
+            check(k)
+        out = []
+        for i in range(k):
+            r = buf[i]
+            row = {"frontier": r.frontier, "edges": r.edges, "overflow": r.overflow, "pieces": r.pieces,
+                   "probe": r.probe}
+            if r.last_done_ns:
+                row["us_work"] = (r.last_done_ns - r.start_ns) / 1e3
+                row["us_spread"] = (r.last_done_ns - r.first_done_ns) / 1e3
+                if i + 1 < k:
+                    row["us_barrier"] = (buf[i + 1].start_ns - r.last_done_ns) / 1e3
+            out.append(row)
+        return out
 
     def autotune(self, sources) -> Opts:
         s = np.ascontiguousarray(sources, dtype=np.int32)

@@ -213,6 +213,26 @@ int dfq_bfs_last_stats(dfq_graph* g, dfq_stats* stats);
  * bfs_ftr_prof.cu:98-144, printed from the device at :206-208). */
 int dfq_bfs_last_trace(dfq_graph* g, int64_t* start_ns, int32_t* frontier, int32_t max_levels);
 
+/* Per-level profile of the last completed launch (first 64 levels): what the
+ * level scanned and how it ended.  start_ns..last_done_ns are device clock
+ * readings: last_done - first_done is the spread of block finish times (load
+ * imbalance) and the next level's start_ns - last_done_ns the barrier's cost.
+ * Replaces the reference's device-printf profilers (bfs_ftr_prof.cu:98-144 and
+ * design/shared-q/atomic-sa/sup-sep/upper-bound/profile/workload.cuh), which print
+ * per-bin frontier sizes and visit counts from inside the kernel. */
+typedef struct dfq_level_info {
+    int64_t start_ns;       /* %globaltimer when the level began (block 0, after the barrier) */
+    int64_t first_done_ns;  /* earliest block to finish the level's work */
+    int64_t last_done_ns;   /* latest block to finish it */
+    int32_t frontier;       /* frontier entries expanded (local + overflow + large) */
+    int32_t edges;          /* their degree sum: adjacency entries the level scans */
+    int32_t overflow;       /* entries read from the global overflow queue */
+    int32_t pieces;         /* large-list pieces */
+    int32_t probe;          /* 1: probe-then-claim level, 0: claim at once */
+    int32_t pad;
+} dfq_level_info;
+int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels);
+
 /* Choose opts for this graph by timing candidate settings on a few sources;
  * writes the winner to *best and installs it on the graph. */
 int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, dfq_opts* best);

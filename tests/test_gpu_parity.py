@@ -145,6 +145,41 @@ def test_rmat18_several_sources():
             run_and_check(g, int(s), graph=dg)
 
 
+@pytest.mark.parametrize("kind", ["rmat", "grid"])
+def test_level_profile_matches_oracle(kind):
+    """The per-level profile counts what the oracle's levels imply: level L
+    expands the vertices at depth L with out-degree > 0 and scans their
+    degree sum; device clock readings are ordered."""
+    if kind == "rmat":
+        g = d.gen_rmat(16, 16, seed=12)
+        src = int(g.pick_sources(1, seed=12)[0])
+    else:
+        g, _ = d.gen_grid(128, 0.01, seed=12)
+        src = 0
+    want = oracle.bfs(g.offsets, g.cols, src)
+    deg = g.degrees()
+    with d.Graph(g) as dg:
+        dg.bfs(src)
+        st = dg.last_stats()
+        prof = dg.last_levels(64)
+        ns, fr = dg.last_trace(64)
+    assert len(prof) == min(64, st.levels + 1) and len(ns) == len(prof)
+    for L, row in enumerate(prof):
+        at = (want == L) & (deg > 0)
+        assert row["frontier"] == int(at.sum()) == fr[L], L
+        if L < st.levels:
+            assert row["edges"] == int(deg[at].sum()), L
+            assert 0 <= row["overflow"] <= row["frontier"]
+            assert row["probe"] in (0, 1)
+            # blocks with nothing to do can finish before block 0 stamps the start
+            assert row["us_work"] >= 0 and row["us_spread"] >= 0
+            if "us_barrier" in row:
+                assert row["us_barrier"] >= 0
+    if st.levels < 64:
+        assert sum(r["edges"] for r in prof) == st.edges
+    assert np.all(np.diff(ns) >= 0)
+
+
 def test_repeated_runs_identical():
     g = d.gen_rmat(15, 16, seed=8)
     src = int(g.pick_sources(1, seed=8)[0])
