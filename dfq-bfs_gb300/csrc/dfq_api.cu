@@ -49,6 +49,14 @@ struct dfq_graph {
     dfqk::Control* ctl = nullptr;
     dfqk::Control* ctl_host = nullptr;  // pinned copy for status / stats
     bool persist_set = false;
+    // hub-first vertex order (when chosen at create): the device CSR uses new
+    // ids, new id rank[v] for input id v, input id order[i] for new id i
+    bool relabeled = false;
+    std::vector<int32_t> rank_host;
+    int32_t* rank = nullptr;
+    int32_t* order = nullptr;
+    int32_t* levels_int = nullptr;   // levels / parents by new id
+    int32_t* parents_int = nullptr;
 };
 
 namespace {
@@ -82,9 +90,12 @@ int validate_opts(const dfq_opts& o) {
     if (o.local_edge_budget < 0) return fail(DFQ_EINVAL, "local_edge_budget must be >= 0");
     if (o.timeout_ms < 1) return fail(DFQ_EINVAL, "timeout_ms must be >= 1");
     if (o.probe_first < 0 || o.probe_first > 2) return fail(DFQ_EINVAL, "probe_first must be 0, 1 or 2");
+    if (o.hot_cache != 0 && o.hot_cache != -1) return fail(DFQ_EINVAL, "hot_cache must be 0 or -1");
+    if (o.vertex_order < 0 || o.vertex_order > 2) return fail(DFQ_EINVAL, "vertex_order must be 0, 1 or 2");
     const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true);
-    if (L.bytes > 200 * 1024)
-        return fail(DFQ_EINVAL, "options need %d bytes of shared memory per block (max 204800)", L.bytes);
+    const int need = L.bytes + (o.hot_cache == 0 ? 4 * dfqk::kHotWordsMax : 0);
+    if (need > 227 * 1024)
+        return fail(DFQ_EINVAL, "options need %d bytes of shared memory per block (max 232448)", need);
     return DFQ_OK;
 }
 
@@ -118,6 +129,26 @@ __global__ void validate_csr_kernel(const int32_t* off, const int32_t* cols, int
     if (tid == 0 && (off[0] != 0 || (int64_t)off[n] != e)) atomicCAS(bad, 0, 2);
     for (int64_t k = tid; k < e; k += nth)
         if ((uint32_t)cols[k] >= (uint32_t)n) atomicCAS(bad, 0, 3);
+}
+
+// In-degree of every vertex (appearances in cols).
+__global__ void indegree_kernel(const int32_t* __restrict__ cols, int64_t e, int32_t* __restrict__ indeg) {
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < e; k += nth) atomicAdd(&indeg[cols[k]], 1);
+}
+
+// Rows of the relabelled graph: new vertex i is input vertex order[i]; its
+// neighbours are that row's, renamed through rank.  One warp per row.
+__global__ void relabel_rows_kernel(const int32_t* __restrict__ off_in, const int32_t* __restrict__ cols_in,
+                                    const int32_t* __restrict__ off_new, const int32_t* __restrict__ order,
+                                    const int32_t* __restrict__ rank, int32_t n, int32_t* __restrict__ cols_new) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
+        const int32_t o = order[i];
+        const int32_t s0 = off_in[o], d = off_in[o + 1] - s0, t = off_new[i];
+        for (int32_t k = lane; k < d; k += 32) cols_new[t + k] = rank[cols_in[s0 + k]];
+    }
 }
 
 int map_device_status(const dfqk::Control& c) {
@@ -154,6 +185,10 @@ void release(dfq_graph* g) {
         cudaFree(g->piece_v[i]);
     }
     cudaFree(g->ctl);
+    cudaFree(g->rank);
+    cudaFree(g->order);
+    cudaFree(g->levels_int);
+    cudaFree(g->parents_int);
     if (g->ctl_host) cudaFreeHost(g->ctl_host);
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
@@ -187,6 +222,94 @@ int apply_persist(dfq_graph* g) {
     return DFQ_OK;
 }
 
+// Hub-first order: input ids sorted by descending in-degree, ties by id
+// (a stable counting sort), so the most-probed vertices get the smallest
+// ids.  Chosen automatically when the graph has at least 2^16 vertices and
+// its largest in-degree is at least 64 times the average.
+bool want_hub_first(const std::vector<int32_t>& indeg, int32_t n, int64_t e, int mode) {
+    if (mode == 1) return false;
+    if (mode == 2) return true;
+    if (n < (1 << 16)) return false;
+    const int32_t mx = *std::max_element(indeg.begin(), indeg.end());
+    return (double)mx >= 64.0 * ((double)e / (double)n);
+}
+
+void hub_first_order(const std::vector<int32_t>& indeg, int32_t n, std::vector<int32_t>& order) {
+    const int32_t mx = *std::max_element(indeg.begin(), indeg.end());
+    order.resize(n);
+    if ((int64_t)mx <= 4 * (int64_t)n + 1024) {
+        std::vector<int64_t> at((size_t)mx + 2, 0);  // at[k]: first slot of in-degree mx - k
+        for (int32_t v = 0; v < n; ++v) at[(size_t)(mx - indeg[v]) + 1]++;
+        for (size_t k = 1; k < at.size(); ++k) at[k] += at[k - 1];
+        for (int32_t v = 0; v < n; ++v) order[at[(size_t)(mx - indeg[v])]++] = v;
+    } else {
+        for (int32_t v = 0; v < n; ++v) order[v] = v;
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return indeg[a] > indeg[b]; });
+    }
+}
+
+// Rewrite g's device CSR in hub-first ids if the options and the graph call
+// for it (g->offsets / g->cols hold the input CSR, validated).
+int maybe_relabel(dfq_graph* g) {
+    const int32_t n = g->n;
+    const int64_t e = g->e;
+    if (g->opts.vertex_order == 1 || e == 0) return DFQ_OK;
+    int32_t* indeg_d = nullptr;
+    int rc = dev_alloc(&indeg_d, (size_t)n);
+    if (rc) return rc;
+    std::vector<int32_t> indeg((size_t)n);
+    cudaMemsetAsync(indeg_d, 0, sizeof(int32_t) * (size_t)n, g->stream);
+    indegree_kernel<<<g->sms * 8, 256, 0, g->stream>>>(g->cols, e, indeg_d);
+    cudaMemcpyAsync(indeg.data(), indeg_d, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, g->stream);
+    cudaError_t err = cudaStreamSynchronize(g->stream);
+    cudaFree(indeg_d);
+    if (err != cudaSuccess) return fail(DFQ_ECUDA, "in-degree count: %s", cudaGetErrorString(err));
+    if (!want_hub_first(indeg, n, e, g->opts.vertex_order)) return DFQ_OK;
+
+    std::vector<int32_t> order, off_in((size_t)n + 1), off_new((size_t)n + 1);
+    hub_first_order(indeg, n, order);
+    std::vector<int32_t> rank((size_t)n);
+    for (int32_t i = 0; i < n; ++i) rank[order[i]] = i;
+    CUDA_TRY(cudaMemcpyAsync(off_in.data(), g->offsets, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost,
+                             g->stream));
+    CUDA_TRY(cudaStreamSynchronize(g->stream));
+    off_new[0] = 0;
+    for (int32_t i = 0; i < n; ++i) off_new[i + 1] = off_new[i] + (off_in[order[i] + 1] - off_in[order[i]]);
+
+    int32_t *off_d = nullptr, *cols_d = nullptr;
+    if ((rc = dev_alloc(&g->rank, (size_t)n)) || (rc = dev_alloc(&g->order, (size_t)n)) ||
+        (rc = dev_alloc(&g->levels_int, (size_t)n)) || (rc = dev_alloc(&off_d, (size_t)n + 1)) ||
+        (rc = dev_alloc(&cols_d, (size_t)e + kColsPad))) {
+        cudaFree(off_d);
+        cudaFree(cols_d);
+        return rc;
+    }
+    CUDA_TRY(cudaMemcpyAsync(g->rank, rank.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, g->stream));
+    CUDA_TRY(cudaMemcpyAsync(g->order, order.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, g->stream));
+    CUDA_TRY(cudaMemcpyAsync(off_d, off_new.data(), sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice,
+                             g->stream));
+    CUDA_TRY(cudaMemsetAsync(cols_d + e, 0, sizeof(int32_t) * kColsPad, g->stream));
+    relabel_rows_kernel<<<g->sms * 8, 256, 0, g->stream>>>(g->offsets, g->cols, off_d, g->order, g->rank, n, cols_d);
+    err = cudaStreamSynchronize(g->stream);
+    if (err != cudaSuccess) {
+        cudaFree(off_d);
+        cudaFree(cols_d);
+        return fail(DFQ_ECUDA, "relabel: %s", cudaGetErrorString(err));
+    }
+    cudaFree(g->offsets);
+    cudaFree(g->cols);
+    g->offsets = off_d;
+    g->cols = cols_d;
+    g->rank_host = std::move(rank);
+    g->relabeled = true;
+    return DFQ_OK;
+}
+
+// Shared-memory words of the hot-vertex cache for a graph of bitmap_words.
+int hot_words_for(const dfq_opts& o, int n) {
+    return o.hot_cache != 0 ? 0 : dfqk::hot_words_of(dfqk::kHotWordsMax, n);
+}
+
 // Queue control-block reset + the cooperative kernel on g->stream.
 int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     const dfq_opts& o = g->opts;
@@ -194,9 +317,11 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     KernelFn k = pick_kernel(o.block_threads, par);
     if (!k) return fail(DFQ_EINVAL, "no kernel for block_threads=%d", o.block_threads);
     const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
-    CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.bytes));
+    const int hot_words = hot_words_for(o, g->n);
+    const int smem = lay.bytes + 4 * hot_words;
+    CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k, o.block_threads, lay.bytes));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k, o.block_threads, smem));
     if (per_sm < 1) return fail(DFQ_EINVAL, "kernel does not fit on an SM with these options");
     if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
     const int grid = g->sms * per_sm;
@@ -228,11 +353,24 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     p.probe_first = o.probe_first;
     p.use_tma = o.use_tma;
     p.timeout_ns = (long long)o.timeout_ms * 1000000LL;
+    p.hot_words = hot_words;
+    if (g->relabeled) {
+        if (par && !g->parents_int) {
+            int rc = dev_alloc(&g->parents_int, (size_t)g->n);
+            if (rc) return rc;
+        }
+        p.src = g->rank_host[src];
+        p.levels = g->levels_int;
+        p.parents = par ? g->parents_int : nullptr;
+        p.levels_out = levels;
+        p.parents_out = parents;
+        p.rank = g->rank;
+        p.order = g->order;
+    }
 
     CUDA_TRY(cudaMemsetAsync(g->ctl, 0, sizeof(dfqk::Control), g->stream));
     void* args[] = {&p};
-    CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(o.block_threads), args, lay.bytes,
-                                         g->stream));
+    CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(o.block_threads), args, smem, g->stream));
     return DFQ_OK;
 }
 
@@ -283,6 +421,8 @@ void dfq_opts_default(dfq_opts* o) {
     o->timeout_ms = 5000;
     o->wide_min_edges = 1 << 21;
     o->wide_min_degree = 8;
+    o->hot_cache = 0;
+    o->vertex_order = 0;
 }
 
 int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int64_t e, const dfq_opts* opts,
@@ -365,6 +505,7 @@ int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int
                                                                                   : "a column index is outside [0,n)");
         }
     }
+    G_TRY(maybe_relabel(g));
     G_TRY(apply_persist(g));
     G_CUDA(cudaStreamSynchronize(g->stream));
 #undef G_TRY

@@ -44,11 +44,13 @@ struct BatchParams {
     WsLayout block_lay;       // layout of each of them
     int medium_min, large_min, piece_edges, local_cap, local_budget, probe_first, use_tma;
     long long timeout_ns;
+    int hot_words;  // hot-vertex cache words this launch reserves (0: none)
 };
 
 __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, int qi, const Workspace& ws) {
     const BatchQuery& q = bp.queries[qi];
     const PoolGraph& g = bp.graphs[q.graph];
+    sp = Params{};  // shared memory starts undefined: every field not set below is zero / null
     sp.offsets = g.offsets;
     sp.cols = g.cols;
     sp.n = g.n;
@@ -74,6 +76,7 @@ __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, i
     sp.probe_first = bp.probe_first;
     sp.use_tma = bp.use_tma;
     sp.timeout_ns = bp.timeout_ns;
+    sp.hot_words = hot_words_of(bp.hot_words, g.n);
 }
 
 // This block's narrow-query workspace.
@@ -342,8 +345,10 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     const void* fn = pick_single(o.block_threads, par);
     if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
     const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
+    const int hot = o.hot_cache == 0 ? hot_words_of(kHotWordsMax, p->n[graph]) : 0;
+    const int smem = lay.bytes + 4 * hot;
     int grid = 0;
-    if ((rc = grid_for(p, fn, o.block_threads, lay.bytes, &grid))) return rc;
+    if ((rc = grid_for(p, fn, o.block_threads, smem, &grid))) return rc;
     const Workspace w = ws_from(p->wide_mem, p->wide_lay);
     Params prm;
     memset(&prm, 0, sizeof prm);
@@ -372,9 +377,10 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     prm.probe_first = o.probe_first;
     prm.use_tma = o.use_tma;
     prm.timeout_ns = (long long)o.timeout_ms * 1000000LL;
+    prm.hot_words = hot;
     cudaEventRecord(p->ev0, p->stream);
     cudaMemsetAsync(p->d_ctl1, 0, sizeof(Control), p->stream);
-    if ((rc = launch_coop(fn, grid, o.block_threads, lay.bytes, &prm, p->stream))) return rc;
+    if ((rc = launch_coop(fn, grid, o.block_threads, smem, &prm, p->stream))) return rc;
     cudaEventRecord(p->ev1, p->stream);
     cudaMemcpyAsync(p->h_ctl1, p->d_ctl1, sizeof(Control), cudaMemcpyDeviceToHost, p->stream);
     cudaError_t err = cudaStreamSynchronize(p->stream);
@@ -412,8 +418,14 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     const void* fn = pick_batch(o.block_threads, par);
     if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
     const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
+    // one cache size per pool (the largest graph's), so a captured launch
+    // stays valid for any batch of the same shape
+    int hot = 0;
+    if (o.hot_cache == 0)
+        for (int i = 0; i < p->ngraphs; ++i) hot = std::max(hot, hot_words_of(kHotWordsMax, p->n[i]));
+    const int smem = lay.bytes + 4 * hot;
     int grid = 0, rc;
-    if ((rc = grid_for(p, fn, o.block_threads, lay.bytes, &grid))) return rc;
+    if ((rc = grid_for(p, fn, o.block_threads, smem, &grid))) return rc;
     if ((rc = ensure_wide(p, par))) return rc;
     if ((rc = ensure_blocks(p, grid, par))) return rc;
     if ((rc = ensure_tables(p, nq))) return rc;
@@ -458,6 +470,7 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     bp.probe_first = o.probe_first;
     bp.use_tma = o.use_tma;
     bp.timeout_ns = (long long)o.timeout_ms * 1000000LL;
+    bp.hot_words = hot;
 
     auto enqueue = [&]() -> int {
         cudaError_t e1 = cudaMemcpyAsync(p->d_queries, p->h_queries, sizeof(BatchQuery) * nq, cudaMemcpyHostToDevice, p->stream);
@@ -465,7 +478,7 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
         cudaError_t e3 = cudaMemsetAsync(p->d_ctls, 0, sizeof(Control) * nq, p->stream);
         cudaError_t e4 = cudaMemsetAsync(p->d_misc, 0, 256, p->stream);
         if (e1 || e2 || e3 || e4) return fail(DFQ_ECUDA, "batch upload failed");
-        return launch_coop(fn, grid, o.block_threads, lay.bytes, &bp, p->stream);
+        return launch_coop(fn, grid, o.block_threads, smem, &bp, p->stream);
     };
     cudaEventRecord(p->ev0, p->stream);
     if (flags & DFQ_BATCH_GRAPH) {

@@ -118,6 +118,17 @@ struct Params {
     int probe_first;
     int use_tma;
     long long timeout_ns;
+    // visited bits of vertices [0, 32 * hot_words) cached in shared memory on
+    // probe levels (0: no cache); a multiple of 32 words, at most kHotWordsMax
+    int hot_words;
+    // vertex order: when the graph was relabelled (rank != null) the kernel
+    // runs on new ids, with levels / parents above indexed by new id, and at
+    // the end writes levels_out[v] = levels[rank[v]] and parents_out[v] =
+    // order[parents[rank[v]]] for the caller's ids v
+    const int* rank;
+    const int* order;
+    int* levels_out;
+    int* parents_out;
 };
 
 // Pieces one level can produce with pieces of at least min_piece (>= 64)
@@ -298,6 +309,14 @@ __device__ __forceinline__ bool group_barrier(Control* ctl, int gsize, unsigned&
 
 // ------------------------------------------------------------ shared layout
 constexpr int kRing = 256;  // per-warp candidate ring (entries, power of two)
+constexpr int kHotWordsMax = 8192;  // hot-vertex visited cache: 32 KB, 262,144 vertices
+
+// Hot-cache words for a graph of n vertices under a launch limit: whole
+// 32-word groups of the graph's bitmap (a multiple of 4 for 16-byte copies).
+__host__ __device__ inline int hot_words_of(int limit_words, int n) {
+    const int words = ((n + 31) / 32) & ~31;
+    return words < limit_words ? words : limit_words;
+}
 
 struct SmemLayout {
     int q_off;     // local queues: 2 buffers x {start, deg, v} x cap ints
@@ -305,7 +324,8 @@ struct SmemLayout {
     int ring_off;  // per-warp candidate ring: kRing vertices (+ kRing parents)
     int tma_off;   // per-warp piece buffers: 2 x (piece + 16) ints, 128-byte aligned
     int bar_off;   // per-warp mbarriers: 2 x u64
-    int bytes;
+    int hot_off;   // hot-vertex visited cache (last, so its size changes no other offset)
+    int bytes;     // without the hot cache: a launch adds 4 * hot_words
 };
 __host__ __device__ inline SmemLayout smem_layout(int B, int cap, int piece, bool par) {
     SmemLayout L;
@@ -318,6 +338,8 @@ __host__ __device__ inline SmemLayout smem_layout(int B, int cap, int piece, boo
     L.tma_off = o;  o += NW * 2 * (piece + 16) * 4;
     o = (o + 15) & ~15;
     L.bar_off = o;  o += NW * 2 * 8;
+    o = (o + 15) & ~15;
+    L.hot_off = o;
     L.bytes = o;
     return L;
 }
@@ -343,6 +365,7 @@ struct BlockShared {
     unsigned long long overflow;    // entries this block sent to the overflow queue (whole BFS)
     unsigned long long large;       // entries this block sent to the large queue (whole BFS)
     unsigned long long red[2];
+    int hot_off;                    // byte offset of the hot-vertex cache in dynamic shared memory
 };
 static __shared__ BlockShared sh;
 extern __shared__ __align__(128) unsigned char dfq_smem[];
@@ -355,7 +378,18 @@ struct Lv {
     int qn;     // local queue buffer being filled
     int cap;    // entries this block may keep locally at this level
     int probe;  // probe the bitmap before claiming
+    unsigned hot;  // vertices below this id have visited bits in the shared cache (0: none)
 };
+
+// The block's hot-vertex visited cache (shared memory).  A set bit means the
+// vertex is visited (bits are only ever set); a clear bit means "ask the
+// global bitmap".
+__device__ __forceinline__ unsigned* hot_cache() { return reinterpret_cast<unsigned*>(dfq_smem + sh.hot_off); }
+
+// Record in the shared cache that v is visited (v < lv.hot).
+__device__ __forceinline__ void hot_learn(const Lv& lv, int v) {
+    if ((unsigned)v < lv.hot) atomicOr(&hot_cache()[v >> 5], 1u << (v & 31));
+}
 
 // Per-thread tallies (32-bit: one thread never scans 2^32 edges, e < 2^31).
 struct Tally {
@@ -593,6 +627,7 @@ __device__ __forceinline__ void claim1(const Params& p, const Lv& lv, Tally& t, 
         eo = __ldg(p.offsets + v + 1);
         const unsigned bit = 1u << (v & 31);
         won = !(atomicOr(&p.bitmap[v >> 5], bit) & bit);
+        hot_learn(lv, v);  // visited now, whoever won
     }
     int st[4] = {0, 0, 0, 0}, dg[4] = {0, 0, 0, 0};
     const int vv[4] = {v, 0, 0, 0};
@@ -632,6 +667,21 @@ __device__ __forceinline__ void ring_drain(const Params& p, const Lv& lv, Tally&
     }
 }
 
+// Drop from vm the entries the shared hot-vertex cache already knows to be
+// visited; the rest go on to the global bitmap.
+template <int K>
+__device__ __forceinline__ unsigned hot_filter(const Lv& lv, const int (&v)[K], unsigned vm) {
+    if (!lv.hot) return vm;
+    const unsigned* hc = hot_cache();
+    unsigned hw[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) hw[j] = ((vm >> j & 1) && (unsigned)v[j] < lv.hot) ? hc[v[j] >> 5] : 0u;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+        if ((hw[j] >> (v[j] & 31)) & 1u) vm &= ~(1u << j);
+    return vm;
+}
+
 // Probe levels: test up to four neighbours per lane against the visited
 // bitmap and append the unvisited ones to the warp's ring (prefix-sum
 // compaction); claims happen in full-warp batches in ring_drain.  The ring
@@ -641,14 +691,18 @@ template <bool PAR>
 __device__ __forceinline__ void probe4(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[4],
                                        unsigned vmask, const int (&par)[4]) {
     const int lane = threadIdx.x & 31;
+    t.edges += __popc(vmask);
+    vmask = hot_filter<4>(lv, v, vmask);
     unsigned w[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) w[j] = (vmask >> j & 1) ? p.bitmap[v[j] >> 5] : 0xffffffffu;
     unsigned cm = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
-        if ((vmask >> j & 1) && !((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
-    t.edges += __popc(vmask);
+    for (int j = 0; j < 4; ++j) {
+        if (!(vmask >> j & 1)) continue;
+        if (!((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
+        else hot_learn(lv, v[j]);
+    }
     const int c = __popc(cm);
     int incl = c;
 #pragma unroll
@@ -682,14 +736,18 @@ template <bool PAR>
 __device__ __forceinline__ void probe8(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[8],
                                        unsigned vm, int par0) {
     const int lane = threadIdx.x & 31;
+    t.edges += __popc(vm);
+    vm = hot_filter<8>(lv, v, vm);
     unsigned w[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) w[j] = (vm >> j & 1) ? p.bitmap[v[j] >> 5] : 0xffffffffu;
     unsigned cm = 0;
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
-        if ((vm >> j & 1) && !((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
-    t.edges += __popc(vm);
+    for (int j = 0; j < 8; ++j) {
+        if (!(vm >> j & 1)) continue;
+        if (!((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
+        else hot_learn(lv, v[j]);
+    }
     if (!__any_sync(kFull, cm)) return;
     const int c_lo = __popc(cm & 15u), c_hi = __popc(cm >> 4);
     int incl = c_lo | (c_hi << 16);
@@ -895,6 +953,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         }
     }
     if (tid == 0) {
+        sh.hot_off = lay.hot_off;
         sh.local_pack = 0ull;
         sh.cnt_cur = sh.local_grab = sh.ovf_pushed = sh.large_pushed = sh.claimed = 0;
         sh.ovf_edges = sh.large_edges = 0;
@@ -948,6 +1007,17 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         // where it scans fewer edges than one 4-edge round per lane of the
         // grid; 2 = decide per level
         lv.probe = p.probe_first == 2 ? (sh.in[4] >= 128 * nwarps ? 1 : 0) : p.probe_first;
+        // probe levels consult the shared hot-vertex cache, refreshed here from
+        // the global bitmap (everything visited before this level) and added
+        // to during the level as this block meets visited vertices
+        lv.hot = 0u;
+        if (lv.probe && p.hot_words > 0) {
+            lv.hot = 32u * (unsigned)p.hot_words;
+            const uint4* src4 = reinterpret_cast<const uint4*>(p.bitmap);
+            uint4* dst4 = reinterpret_cast<uint4*>(hot_cache());
+            for (int i = tid; i < (p.hot_words >> 2); i += B) dst4[i] = __ldcg(src4 + i);
+            __syncthreads();
+        }
         if (grank == 0 && tid == 0 && L < kTraceLevels) {
             ctl->trace_edges[L] = sh.in[4];
             ctl->trace_ovf[L] = n_ovf;
@@ -1135,6 +1205,22 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             // recorded after the barrier: its release would otherwise wait for them
             atomicMax(&ctl->trace_done_last[L], done_ns);
             atomicMax(&ctl->trace_done_first[L], ~done_ns);
+        }
+    }
+
+    // ---- relabelled graph: levels (and parents) back to the caller's ids.
+    // Every block passed the final barrier after its last write, so all of
+    // them are visible here (read through L2).
+    if (ok && p.rank) {
+        const long long gtid = (long long)grank * B + tid;
+        const long long nth = (long long)gsize * B;
+        for (long long v = gtid; v < p.n; v += nth) {
+            const int r = __ldg(p.rank + v);
+            p.levels_out[v] = __ldcg(p.levels + r);
+            if (PAR) {
+                const int q = __ldcg(p.parents + r);
+                p.parents_out[v] = q >= 0 ? __ldg(p.order + q) : -1;
+            }
         }
     }
 

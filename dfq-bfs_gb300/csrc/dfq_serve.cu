@@ -96,6 +96,7 @@ struct ServeParams {
     long long join_ns; // ... or its window has been open this long
     int medium_min, large_min, piece_edges, local_cap, local_budget, probe_first, use_tma;
     long long timeout_ns;
+    int hot_words;     // hot-vertex cache words the launch reserves (0: none)
     long long idle_ns;
 };
 
@@ -113,6 +114,7 @@ __device__ __forceinline__ int ld_acquire_sys_s32(const int* p) {
 __device__ __forceinline__ void serve_params(Params& sp, const ServeParams& s, const ServeReq& q, const Workspace& ws,
                                              int ovf_cap, Control* ctl) {
     const PoolGraph& g = s.graphs[q.graph];
+    sp = Params{};  // shared memory starts undefined: every field not set below is zero / null
     sp.offsets = g.offsets;
     sp.cols = g.cols;
     sp.n = g.n;
@@ -138,6 +140,7 @@ __device__ __forceinline__ void serve_params(Params& sp, const ServeParams& s, c
     sp.probe_first = s.probe_first;
     sp.use_tma = s.use_tma;
     sp.timeout_ns = s.timeout_ns;
+    sp.hot_words = hot_words_of(s.hot_words, g.n);
 }
 
 // Copy one ring slot (seq checked: the host writes the fields before the count).
@@ -400,6 +403,7 @@ struct dfq_server {
     size_t block_stride = 0;
     int grid = 0;
     int smem = 0;
+    int hot_words = 0;  // hot-vertex cache words per block (the largest graph's)
     const void* fn = nullptr;
     // HBM arena for per-request outputs: offset -> size of free runs
     unsigned char* arena = nullptr;
@@ -527,6 +531,7 @@ int launch_serve(dfq_server* s) {
     sp.probe_first = o.probe_first;
     sp.use_tma = o.use_tma;
     sp.timeout_ns = (long long)o.timeout_ms * 1000000LL;
+    sp.hot_words = s->hot_words;
     sp.idle_ns = (long long)s->opts.idle_ms * 1000000LL;
     // reset the per-launch state; claim cursors persist across launches
     ServeDev reset;
@@ -645,7 +650,10 @@ int dfq_server_create(dfq_pool* pool, const dfq_server_opts* opts, dfq_server** 
     const dfq_opts& po = pool->opts;
     s->fn = pick_serve(po.block_threads, par);
     if (!s->fn) { server_release_all(s); return fail(DFQ_EINVAL, "block_threads %d", po.block_threads); }
-    s->smem = smem_layout(po.block_threads, po.local_queue_cap, po.piece_edges, par).bytes;
+    s->hot_words = 0;
+    if (po.hot_cache == 0)
+        for (int i = 0; i < pool->ngraphs; ++i) s->hot_words = std::max(s->hot_words, hot_words_of(kHotWordsMax, pool->n[i]));
+    s->smem = smem_layout(po.block_threads, po.local_queue_cap, po.piece_edges, par).bytes + 4 * s->hot_words;
     S_TRY(grid_for(pool, s->fn, po.block_threads, s->smem, &s->grid));
     S_TRY(ensure_wide(pool, par));
     // narrow workspaces: bitmap for the largest narrow graph, bounded queues

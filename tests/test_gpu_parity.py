@@ -180,6 +180,39 @@ def test_level_profile_matches_oracle(kind):
     assert np.all(np.diff(ns) >= 0)
 
 
+@pytest.mark.parametrize("order,hot", [(1, 0), (2, 0), (2, -1), (1, -1)])
+def test_vertex_order_and_hot_cache(order, hot):
+    """Hub-first relabelling and the shared hot-vertex cache change only how
+    the kernel works: levels, parents (in input ids) and E_R stay exact, on
+    the whole grid and in a small graph that the cache covers entirely."""
+    for g, srcs in [(d.gen_rmat(16, 16, seed=21), None), (d.gen_zipf_geometric(50000, 4.7, 2.1, seed=21), [0, 7])]:
+        srcs = srcs or [int(x) for x in g.pick_sources(3, seed=21)]
+        with d.Graph(g, opts=opts(vertex_order=order, hot_cache=hot)) as dg:
+            for s in srcs:
+                run_and_check(g, int(s), graph=dg)
+
+
+def test_hub_first_auto_and_device_input():
+    """Auto mode relabels a skewed graph and keeps a uniform one; a graph
+    created from device arrays relabels the same way."""
+    torch = pytest.importorskip("torch")
+    g = d.gen_rmat(17, 16, seed=22)
+    src = int(g.pick_sources(1, seed=22)[0])
+    off = torch.from_numpy(g.offsets).cuda()
+    col = torch.from_numpy(g.cols).cuda()
+    with d.Graph(off, col, n=g.n, e=g.e, opts=opts(vertex_order=0)) as dg:
+        run_and_check(g, src, graph=dg)
+        lv = torch.empty(g.n, dtype=torch.int32, device="cuda")
+        pa = torch.empty(g.n, dtype=torch.int32, device="cuda")
+        dg.launch(src, lv, pa)
+        dg.sync()
+        want = oracle.bfs(g.offsets, g.cols, src)
+        assert oracle.compare(want, lv.cpu().numpy())["mismatches"] == 0
+        assert oracle.validate_tree(g.offsets, g.cols, src, lv.cpu().numpy(), pa.cpu().numpy()) == 0
+    grid, _ = d.gen_grid(300, 0.01, seed=22)
+    run_and_check(grid, 0, opts(vertex_order=0))
+
+
 def test_repeated_runs_identical():
     g = d.gen_rmat(15, 16, seed=8)
     src = int(g.pick_sources(1, seed=8)[0])
