@@ -90,10 +90,11 @@ int validate_opts(const dfq_opts& o) {
     if (o.local_edge_budget < 0) return fail(DFQ_EINVAL, "local_edge_budget must be >= 0");
     if (o.timeout_ms < 1) return fail(DFQ_EINVAL, "timeout_ms must be >= 1");
     if (o.probe_first < 0 || o.probe_first > 2) return fail(DFQ_EINVAL, "probe_first must be 0, 1 or 2");
-    if (o.hot_cache != 0 && o.hot_cache != -1) return fail(DFQ_EINVAL, "hot_cache must be 0 or -1");
+    if (o.hot_cache < -1 || o.hot_cache > 1) return fail(DFQ_EINVAL, "hot_cache must be -1, 0 or 1");
+    if (o.profile != 0 && o.profile != 1) return fail(DFQ_EINVAL, "profile must be 0 or 1");
     if (o.vertex_order < 0 || o.vertex_order > 2) return fail(DFQ_EINVAL, "vertex_order must be 0, 1 or 2");
     const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true);
-    const int need = L.bytes + (o.hot_cache == 0 ? 4 * dfqk::kHotWordsMax : 0);
+    const int need = L.bytes + (o.hot_cache >= 0 ? 4 * dfqk::kHotWordsMax : 0);
     if (need > 227 * 1024)
         return fail(DFQ_EINVAL, "options need %d bytes of shared memory per block (max 232448)", need);
     return DFQ_OK;
@@ -306,8 +307,9 @@ int maybe_relabel(dfq_graph* g) {
 }
 
 // Shared-memory words of the hot-vertex cache for a graph of bitmap_words.
-int hot_words_for(const dfq_opts& o, int n) {
-    return o.hot_cache != 0 ? 0 : dfqk::hot_words_of(dfqk::kHotWordsMax, n);
+int hot_words_for(const dfq_opts& o, int n, bool hub_first) {
+    const bool on = o.hot_cache == 1 || (o.hot_cache == 0 && hub_first);
+    return on ? dfqk::hot_words_of(dfqk::kHotWordsMax, n) : 0;
 }
 
 // Queue control-block reset + the cooperative kernel on g->stream.
@@ -317,7 +319,7 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     KernelFn k = pick_kernel(o.block_threads, par);
     if (!k) return fail(DFQ_EINVAL, "no kernel for block_threads=%d", o.block_threads);
     const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
-    const int hot_words = hot_words_for(o, g->n);
+    const int hot_words = hot_words_for(o, g->n, g->relabeled);
     const int smem = lay.bytes + 4 * hot_words;
     CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;
@@ -354,6 +356,7 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     p.use_tma = o.use_tma;
     p.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     p.hot_words = hot_words;
+    p.profile = o.profile;
     if (g->relabeled) {
         if (par && !g->parents_int) {
             int rc = dev_alloc(&g->parents_int, (size_t)g->n);
@@ -423,6 +426,7 @@ void dfq_opts_default(dfq_opts* o) {
     o->wide_min_degree = 8;
     o->hot_cache = 0;
     o->vertex_order = 0;
+    o->profile = 0;
 }
 
 int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int64_t e, const dfq_opts* opts,

@@ -121,6 +121,7 @@ struct Params {
     // visited bits of vertices [0, 32 * hot_words) cached in shared memory on
     // probe levels (0: no cache); a multiple of 32 words, at most kHotWordsMax
     int hot_words;
+    int profile;  // 1: record each block's level finish times
     // vertex order: when the graph was relabelled (rank != null) the kernel
     // runs on new ids, with levels / parents above indexed by new id, and at
     // the end writes levels_out[v] = levels[rank[v]] and parents_out[v] =
@@ -219,7 +220,12 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned
         : "memory");
 }
 
+// Set when a thread of this block records an error: a one-block group stops
+// on it without reading the status word back from global memory.
+static __shared__ int s_block_err;
+
 __device__ __forceinline__ void set_error(Control* ctl, int code, int a, int b) {
+    s_block_err = 1;
     if (atomicCAS(&ctl->status, 0, code) == 0) {
         ctl->err_info[0] = a;
         ctl->err_info[1] = b;
@@ -268,16 +274,21 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
                 }
             }
         }
-        if (ok && *(volatile int*)&ctl->status != 0) ok = 0;
-        *s_flag = ok;
         if (ok) {
-            s_in[0] = __ldcg(&next->pushed);
-            s_in[1] = __ldcg(&next->ovf_count);
+            // the status word and the counters in one round of loads
+            const int st = *(volatile int*)&ctl->status;
+            const int pushed = __ldcg(&next->pushed);
+            const int ovf = __ldcg(&next->ovf_count);
             const unsigned long long lp = __ldcg(&next->large_pack);
+            const int edges = __ldcg(&next->pushed_edges);
+            ok = st == 0;
+            s_in[0] = pushed;
+            s_in[1] = ovf;
             s_in[2] = (int)(lp >> 32);
             s_in[3] = (int)(unsigned)lp;
-            s_in[4] = __ldcg(&next->pushed_edges);
+            s_in[4] = edges;
         }
+        *s_flag = ok;
     }
     __syncthreads();
     return *s_flag != 0;
@@ -286,9 +297,16 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
 // Level barrier of a group of blocks running one BFS: the grid barrier above
 // for several blocks; for a one-block group, the block barrier plus thread 0
 // reading the counters its own block's atomics produced.
+// With local_in, a one-block group's thread 0 has already written the next
+// level's input into s_in from the block's own shared tallies (they are the
+// whole group's), so the barrier is just the block barrier.
 __device__ __forceinline__ bool group_barrier(Control* ctl, int gsize, unsigned& target, long long timeout_ns,
-                                              int* s_flag, const LevelCtr* next, int* s_in) {
+                                              int* s_flag, const LevelCtr* next, int* s_in, bool local_in) {
     if (gsize > 1) return grid_barrier(ctl, target, timeout_ns, s_flag, next, s_in, gsize);
+    if (local_in) {
+        __syncthreads();
+        return s_block_err == 0;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence_block();
@@ -356,6 +374,7 @@ struct BlockShared {
     int local_grab;                 // cursor over it (32 entries per warp grab)
     int ovf_pushed;                 // entries this block sent to the overflow queue
     int large_pushed;               // entries this block sent to the large queue
+    int large_pieces;               // pieces of those entries
     int claimed;                    // this block claimed a vertex at this level
     int flag;                       // barrier verdict
     int in[5];                      // this level's input: pushed, overflow, large entries, pieces, edges
@@ -515,6 +534,7 @@ __device__ __forceinline__ void push_large(const Params& p, const Lv& lv, unsign
             atomicAdd(&p.ctl->lv[lv.cslot].large_pack, ((unsigned long long)totc << 32) | totp);
         base = (unsigned)old;
         atomicAdd(&sh.large_pushed, (int)totc);
+        atomicAdd(&sh.large_pieces, (int)totp);
         atomicAdd(&sh.large_edges, (int)totd);
         if (base + totp > (unsigned)p.piece_cap) set_error(p.ctl, kErrQueueCap, (int)base, (int)totp);
     }
@@ -953,9 +973,10 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         }
     }
     if (tid == 0) {
+        s_block_err = 0;
         sh.hot_off = lay.hot_off;
         sh.local_pack = 0ull;
-        sh.cnt_cur = sh.local_grab = sh.ovf_pushed = sh.large_pushed = sh.claimed = 0;
+        sh.cnt_cur = sh.local_grab = sh.ovf_pushed = sh.large_pushed = sh.large_pieces = sh.claimed = 0;
         sh.ovf_edges = sh.large_edges = 0;
         sh.depth = 0;
         sh.overflow = sh.large = 0ull;
@@ -967,7 +988,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
     int L = 0;
     Tally t{0u, 0u};
 
-    bool ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[0], sh.in);
+    bool ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[0], sh.in, false);
 
     for (; ok; ++L) {
         const int pushed = sh.in[0];
@@ -1180,15 +1201,23 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
 
         // end of level: publish how much this block pushed, keep its queue
         __syncthreads();
-        unsigned long long done_ns = 0;  // when this block finished the level (thread 0)
+        unsigned long long done_ns = 0;  // when this block finished the level (thread 0, profiling)
         if (tid == 0) {
-            done_ns = globaltimer();
+            if (p.profile) done_ns = globaltimer();
             const int kept = (int)(sh.local_pack >> 32);
             const int tot = kept + sh.ovf_pushed + sh.large_pushed;
-            if (tot) {
+            const int tot_edges = (int)(unsigned)sh.local_pack + sh.ovf_edges + sh.large_edges;
+            if (gsize == 1) {
+                // a one-block group: what this block pushed is the next level's
+                // whole input (the barrier reads nothing back from global memory)
+                sh.in[0] = tot;
+                sh.in[1] = sh.ovf_pushed;
+                sh.in[2] = sh.large_pushed;
+                sh.in[3] = sh.large_pieces;
+                sh.in[4] = tot_edges;
+            } else if (tot) {
                 atomicAdd(&ctl->lv[lv.cslot].pushed, tot);
-                atomicAdd(&ctl->lv[lv.cslot].pushed_edges,
-                          (int)(unsigned)sh.local_pack + sh.ovf_edges + sh.large_edges);
+                atomicAdd(&ctl->lv[lv.cslot].pushed_edges, tot_edges);
             }
             if (sh.claimed) sh.depth = L + 1;
             sh.overflow += (unsigned long long)sh.ovf_pushed;
@@ -1196,12 +1225,12 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             sh.cnt_cur = kept;
             sh.local_pack = 0ull;
             sh.local_grab = 0;
-            sh.ovf_pushed = sh.large_pushed = sh.claimed = 0;
+            sh.ovf_pushed = sh.large_pushed = sh.large_pieces = sh.claimed = 0;
             sh.ovf_edges = sh.large_edges = 0;
         }
         cur ^= 1;
-        ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in);
-        if (tid == 0 && L < kTraceLevels) {
+        ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in, true);
+        if (p.profile && tid == 0 && L < kTraceLevels) {
             // recorded after the barrier: its release would otherwise wait for them
             atomicMax(&ctl->trace_done_last[L], done_ns);
             atomicMax(&ctl->trace_done_first[L], ~done_ns);

@@ -105,9 +105,10 @@ int setup_device(int dev, const dfq_opts& o, DeviceSetup** out) {
         const void* fns[2] = {(const void*)dfqk::dfq_bfs_kernel<kBlock, false>,
                               (const void*)dfqk::dfq_bfs_kernel<kBlock, true>};
         for (int i = 0; i < 2; ++i) {
-            // room for the largest hot-vertex cache, whatever the graph
+            // input ids are kept here, so the hot-vertex cache stays off (as
+            // hot_cache = 0 leaves it for graphs not given hub-first ids)
             const dfqk::SmemLayout lay = dfqk::smem_layout(kBlock, o.local_queue_cap, o.piece_edges, i == 1);
-            d.smem[i] = lay.bytes + 4 * dfqk::kHotWordsMax;
+            d.smem[i] = lay.bytes;
             err = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem[i]);
             int per_sm = 0;
             if (err == cudaSuccess)
@@ -190,7 +191,6 @@ extern "C" int dfq_bfs_noalloc(const int32_t* offsets, const int32_t* cols, int3
     p.probe_first = o.probe_first;
     p.use_tma = o.use_tma;
     p.timeout_ns = (long long)o.timeout_ms * 1000000LL;
-    p.hot_words = dfqk::hot_words_of(dfqk::kHotWordsMax, n);
     const bool par = parents != nullptr;
     const void* fn = par ? (const void*)dfqk::dfq_bfs_kernel<kBlock, true> : (const void*)dfqk::dfq_bfs_kernel<kBlock, false>;
     void* args[] = {&p};

@@ -83,6 +83,23 @@ def test_batch_with_parents(torch):
         check_results(qs, meta, res, parents=True)
 
 
+@pytest.mark.parametrize("flags", [0, d.BATCH_GRAPH])
+def test_batch_with_hot_cache(torch, flags):
+    """The shared hot-vertex cache in both group shapes (whole grid and one
+    block), with parents: same levels, valid trees."""
+    graphs = mixed_graphs()
+    o = opts_small_wide()
+    o.hot_cache = 1
+    with d.Pool(graphs, o) as pool:
+        qs, meta = make_queries(torch, graphs, 2, seed=5, parents=True)
+        res, _ = pool.batch(qs, flags)
+        check_results(qs, meta, res, parents=True)
+        for gi, g in enumerate(graphs[:4]):
+            lv = torch.empty(g.n, dtype=torch.int32, device="cuda")
+            pool.bfs(gi, 0, lv)
+            assert np.array_equal(lv.cpu().numpy(), oracle.bfs(g.offsets, g.cols, 0))
+
+
 def test_batch_all_narrow_and_all_wide(torch):
     graphs = [d.gen_rmat(11, 16, seed=7), d.gen_grid(64, 0.0, seed=1)[0]]
     for wide_edges in (1 << 30, 1):

@@ -158,7 +158,7 @@ def test_level_profile_matches_oracle(kind):
         src = 0
     want = oracle.bfs(g.offsets, g.cols, src)
     deg = g.degrees()
-    with d.Graph(g) as dg:
+    with d.Graph(g, opts=opts(profile=1)) as dg:
         dg.bfs(src)
         st = dg.last_stats()
         prof = dg.last_levels(64)
@@ -180,7 +180,7 @@ def test_level_profile_matches_oracle(kind):
     assert np.all(np.diff(ns) >= 0)
 
 
-@pytest.mark.parametrize("order,hot", [(1, 0), (2, 0), (2, -1), (1, -1)])
+@pytest.mark.parametrize("order,hot", [(1, 0), (2, 0), (2, -1), (1, 1), (2, 1)])
 def test_vertex_order_and_hot_cache(order, hot):
     """Hub-first relabelling and the shared hot-vertex cache change only how
     the kernel works: levels, parents (in input ids) and E_R stay exact, on
