@@ -31,18 +31,49 @@
 
 namespace {
 
-void usage() {
-    fprintf(stderr,
-            "usage: bfs <graph> [source] [--ref-compat] [--symmetrize] [--parents] [--no-check]\n"
-            "           [--repeat K] [--autotune] [--json] [--save-bin PATH] [$]\n");
-}
-
 bool is_int(const char* s) {
     if (!*s) return false;
     for (const char* p = (*s == '-' ? s + 1 : s); *p; ++p)
         if (*p < '0' || *p > '9') return false;
     return true;
 }
+bool is_int_prefix(const char* s) { return is_int(s) && strlen(s) < 11; }
+
+void usage() {
+    fprintf(stderr,
+            "usage: bfs <graph> [source] [--ref-compat] [--symmetrize] [--parents] [--no-check]\n"
+            "           [--repeat K] [--autotune] [--json] [--save-bin PATH] [--opt NAME=VALUE]... [$]\n"
+            "  --opt sets one field of dfq_opts (include/dfq.h), e.g. --opt probe_first=0;\n"
+            "  the reference's design variants are separate programs, here they are options\n");
+}
+
+// dfq_opts fields settable with --opt NAME=VALUE.
+struct OptField {
+    const char* name;
+    int32_t dfq_opts::*field;
+};
+const OptField kOptFields[] = {
+    {"block_threads", &dfq_opts::block_threads},       {"blocks_per_sm", &dfq_opts::blocks_per_sm},
+    {"medium_min_degree", &dfq_opts::medium_min_degree}, {"large_min_degree", &dfq_opts::large_min_degree},
+    {"local_queue_cap", &dfq_opts::local_queue_cap},   {"local_edge_budget", &dfq_opts::local_edge_budget},
+    {"piece_edges", &dfq_opts::piece_edges},           {"probe_first", &dfq_opts::probe_first},
+    {"l2_persist", &dfq_opts::l2_persist},             {"use_tma", &dfq_opts::use_tma},
+    {"timeout_ms", &dfq_opts::timeout_ms},             {"hot_cache", &dfq_opts::hot_cache},
+    {"vertex_order", &dfq_opts::vertex_order},
+};
+
+// Apply "NAME=VALUE" to o; false if the name or the value is not recognised.
+bool set_opt(dfq_opts& o, const char* kv) {
+    const char* eq = strchr(kv, '=');
+    if (!eq || !is_int_prefix(eq + 1)) return false;
+    for (const OptField& f : kOptFields)
+        if (strlen(f.name) == (size_t)(eq - kv) && !strncmp(f.name, kv, eq - kv)) {
+            o.*(f.field) = (int32_t)atoi(eq + 1);
+            return true;
+        }
+    return false;
+}
+
 
 // The reference's serial CPU BFS (DFQ:218-253): frontier walked back to front.
 void cpu_bfs(const dfq_csr& g, int32_t src, std::vector<int32_t>& lv) {
@@ -73,6 +104,8 @@ int main(int argc, char** argv) {
     const char* save_bin = nullptr;
     long long src_arg = -1;
     const bool interactive = argv[argc - 1][0] == '$';
+    dfq_opts opts;
+    dfq_opts_default(&opts);
     for (int i = 2; i < argc; ++i) {
         const char* a = argv[i];
         if (interactive && i == argc - 1) continue;
@@ -84,6 +117,12 @@ int main(int argc, char** argv) {
         else if (!strcmp(a, "--autotune")) autotune = true;
         else if (!strcmp(a, "--repeat") && i + 1 < argc) repeat = atoi(argv[++i]);
         else if (!strcmp(a, "--save-bin") && i + 1 < argc) save_bin = argv[++i];
+        else if (!strcmp(a, "--opt") && i + 1 < argc) {
+            if (!set_opt(opts, argv[++i])) {
+                fprintf(stderr, "bfs: --opt '%s': not NAME=INTEGER with a dfq_opts field name\n", argv[i]);
+                return 2;
+            }
+        }
         else if (i == 2 && is_int(a)) src_arg = atoll(a);
         else if (!strcmp(a, "-h") || !strcmp(a, "--help")) { usage(); return 0; }
         else { fprintf(stderr, "bfs: unknown argument '%s'\n", a); usage(); return 2; }
@@ -106,7 +145,7 @@ int main(int argc, char** argv) {
     if (src_arg >= 0 && !ref_compat) source = (int32_t)src_arg;
 
     dfq_graph* dg = nullptr;
-    rc = dfq_graph_create(g.offsets, g.cols, g.n, g.e, nullptr, &dg);
+    rc = dfq_graph_create(g.offsets, g.cols, g.n, g.e, &opts, &dg);
     if (rc) { fprintf(stderr, "bfs: %s\n", dfq_last_error()); printf("\033[0m"); dfq_csr_free(&g); return 1; }
 
     std::vector<int32_t> levels(g.n), parents(want_parents ? g.n : 0), cpu;
