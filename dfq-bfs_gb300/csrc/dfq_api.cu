@@ -51,6 +51,7 @@ struct dfq_graph {
     bool persist_set = false;
     // hub-first vertex order (when chosen at create): the device CSR uses new
     // ids, new id rank[v] for input id v, input id order[i] for new id i
+    bool symmetric = false;  // checked at create when direction = 1 was asked for
     bool relabeled = false;
     std::vector<int32_t> rank_host;
     int32_t* rank = nullptr;
@@ -92,6 +93,7 @@ int validate_opts(const dfq_opts& o) {
     if (o.probe_first < 0 || o.probe_first > 2) return fail(DFQ_EINVAL, "probe_first must be 0, 1 or 2");
     if (o.hot_cache < -1 || o.hot_cache > 1) return fail(DFQ_EINVAL, "hot_cache must be -1, 0 or 1");
     if (o.profile != 0 && o.profile != 1) return fail(DFQ_EINVAL, "profile must be 0 or 1");
+    if (o.direction != 0 && o.direction != 1) return fail(DFQ_EINVAL, "direction must be 0 or 1");
     if (o.vertex_order < 0 || o.vertex_order > 2) return fail(DFQ_EINVAL, "vertex_order must be 0, 1 or 2");
     const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true);
     const int need = L.bytes + (o.hot_cache >= 0 ? 4 * dfqk::kHotWordsMax : 0);
@@ -148,7 +150,47 @@ __global__ void relabel_rows_kernel(const int32_t* __restrict__ off_in, const in
     for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
         const int32_t o = order[i];
         const int32_t s0 = off_in[o], d = off_in[o + 1] - s0, t = off_new[i];
-        for (int32_t k = lane; k < d; k += 32) cols_new[t + k] = rank[cols_in[s0 + k]];
+        int32_t best = INT32_MAX, at = -1;
+        for (int32_t k = lane; k < d; k += 32) {
+            const int32_t c = rank[cols_in[s0 + k]];
+            cols_new[t + k] = c;
+            if (c < best) { best = c; at = k; }
+        }
+        // the row's hub (smallest new id) first: a bottom-up search tries it first
+        for (int off = 16; off > 0; off >>= 1) {
+            const int32_t ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const int32_t oa = __shfl_xor_sync(0xffffffffu, at, off);
+            if (ob < best || (ob == best && oa < at)) { best = ob; at = oa; }
+        }
+        __syncwarp();
+        if (lane == 0 && at > 0) {
+            cols_new[t + at] = cols_new[t];
+            cols_new[t] = best;
+        }
+    }
+}
+
+// Undirected-graph check for direction-optimising BFS: every row sorted
+// (flag bit 2 otherwise) and every edge u->v matched by v->u (bit 1
+// otherwise, found by binary search in row v).  One warp per row.
+__global__ void symmetric_check_kernel(const int32_t* __restrict__ off, const int32_t* __restrict__ cols, int32_t n,
+                                       int* __restrict__ flag) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += nw) {
+        const int32_t s0 = off[u], e0 = off[u + 1];
+        for (int32_t k = s0 + lane; k < e0; k += 32) {
+            const int32_t v = cols[k];
+            if (k + 1 < e0 && cols[k + 1] < v) atomicOr(flag, 2);
+            int32_t lo = off[v], hi = off[v + 1];
+            const int32_t end = hi;
+            while (lo < hi) {
+                const int32_t mid = lo + ((hi - lo) >> 1);
+                if (cols[mid] < (int32_t)u) lo = mid + 1;
+                else hi = mid;
+            }
+            if (lo >= end || cols[lo] != (int32_t)u) atomicOr(flag, 1);
+        }
     }
 }
 
@@ -306,6 +348,24 @@ int maybe_relabel(dfq_graph* g) {
     return DFQ_OK;
 }
 
+// direction = 1 at create: the input CSR must be undirected with sorted rows.
+int check_symmetric(dfq_graph* g) {
+    int* flag = nullptr;
+    int rc = dev_alloc(&flag, 1);
+    if (rc) return rc;
+    int h = 0;
+    cudaMemsetAsync(flag, 0, sizeof(int), g->stream);
+    symmetric_check_kernel<<<g->sms * 8, 256, 0, g->stream>>>(g->offsets, g->cols, g->n, flag);
+    cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+    cudaError_t err = cudaStreamSynchronize(g->stream);
+    cudaFree(flag);
+    if (err != cudaSuccess) return fail(DFQ_ECUDA, "symmetry check: %s", cudaGetErrorString(err));
+    if (h & 2) return fail(DFQ_EINVAL, "direction = 1 needs sorted rows (sort and de-duplicate them, DFQ_CSR_DEDUP)");
+    if (h & 1) return fail(DFQ_EINVAL, "direction = 1 needs an undirected graph: an edge u->v has no v->u");
+    g->symmetric = true;
+    return DFQ_OK;
+}
+
 // Shared-memory words of the hot-vertex cache for a graph of bitmap_words.
 int hot_words_for(const dfq_opts& o, int n, bool hub_first) {
     const bool on = o.hot_cache == 1 || (o.hot_cache == 0 && hub_first);
@@ -357,6 +417,10 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     p.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     p.hot_words = hot_words;
     p.profile = o.profile;
+    if (o.direction == 1 && !g->symmetric)
+        return fail(DFQ_EINVAL, "direction = 1 needs a graph created with direction = 1 (checked undirected)");
+    p.direction = o.direction;
+    p.e = (int)g->e;
     if (g->relabeled) {
         if (par && !g->parents_int) {
             int rc = dev_alloc(&g->parents_int, (size_t)g->n);
@@ -427,6 +491,7 @@ void dfq_opts_default(dfq_opts* o) {
     o->hot_cache = 0;
     o->vertex_order = 0;
     o->profile = 0;
+    o->direction = 0;
 }
 
 int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int64_t e, const dfq_opts* opts,
@@ -509,6 +574,7 @@ int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int
                                                                                   : "a column index is outside [0,n)");
         }
     }
+    if (o.direction == 1) G_TRY(check_symmetric(g));
     G_TRY(maybe_relabel(g));
     G_TRY(apply_persist(g));
     G_CUDA(cudaStreamSynchronize(g->stream));

@@ -122,6 +122,8 @@ struct Params {
     // probe levels (0: no cache); a multiple of 32 words, at most kHotWordsMax
     int hot_words;
     int profile;  // 1: record each block's level finish times
+    int direction;  // 1: levels may run bottom-up (undirected graph, checked by the host)
+    int e;          // edges (the bottom-up switch compares against the unexplored ones)
     // vertex order: when the graph was relabelled (rank != null) the kernel
     // runs on new ids, with levels / parents above indexed by new id, and at
     // the end writes levels_out[v] = levels[rank[v]] and parents_out[v] =
@@ -398,6 +400,7 @@ struct Lv {
     int cap;    // entries this block may keep locally at this level
     int probe;  // probe the bitmap before claiming
     unsigned hot;  // vertices below this id have visited bits in the shared cache (0: none)
+    int bottom_up; // this level: every unvisited vertex looks for a parent in the frontier
 };
 
 // The block's hot-vertex visited cache (shared memory).  A set bit means the
@@ -904,6 +907,67 @@ __device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tall
     }
 }
 
+// Bottom-up level: every unvisited vertex v looks among its neighbours for
+// one at the current level; the first found becomes its parent.  A lane
+// checks its own vertex's first 32 neighbours (with hub-first ids the row's
+// hub comes first); lists still unresolved after that are finished by the
+// whole warp, 32 neighbours at a time.  Only v's lane writes v, so no claim
+// atomics are needed; levels are read through L2 (other blocks wrote this
+// level's).  Found vertices are pushed like claims, so the next level can run
+// either way.  Warp-collective.
+template <bool PAR>
+__device__ __forceinline__ void bottom_up_level(const Params& p, const Lv& lv, Tally& t, int gwarp, int nwarps) {
+    const int lane = threadIdx.x & 31;
+    const int L = lv.next - 1;
+    for (int base = gwarp * 32; base < p.n; base += nwarps * 32) {
+        const int v = base + lane;
+        int s0 = 0, e0 = 0, par = -1;
+        bool open = false;
+        if (v < p.n && __ldcg(p.levels + v) == -1) {
+            s0 = __ldg(p.offsets + v);
+            e0 = __ldg(p.offsets + v + 1);
+            const int lim = min(e0, s0 + 32);
+            for (int k = s0; k < lim; ++k) {
+                const int u = __ldg(p.cols + k);
+                if (__ldcg(p.levels + u) == L) { par = u; break; }
+            }
+            open = par < 0 && e0 > s0 + 32;
+        }
+        unsigned rest = __ballot_sync(kFull, open);
+        while (rest) {  // long lists, one at a time with the whole warp
+            const int i = __ffs(rest) - 1;
+            rest &= rest - 1;
+            const int rs = __shfl_sync(kFull, s0, i) + 32, re = __shfl_sync(kFull, e0, i);
+            int got = -1;
+            for (int k0 = rs; k0 < re && got < 0; k0 += 32) {
+                const int k = k0 + lane;
+                const int u = k < re ? __ldg(p.cols + k) : -1;
+                const bool hit = u >= 0 && __ldcg(p.levels + u) == L;
+                const unsigned hm = __ballot_sync(kFull, hit);
+                if (hm) got = __shfl_sync(kFull, u, __ffs(hm) - 1);
+            }
+            if (lane == i) par = got;
+        }
+        const bool found = par >= 0;
+        int st[4] = {0, 0, 0, 0}, dg[4] = {0, 0, 0, 0};
+        const int vv[4] = {v, 0, 0, 0};
+        unsigned loc = 0, lm = 0;
+        if (found) {
+            p.levels[v] = lv.next;
+            if (PAR) p.parents[v] = par;
+            atomicOr(&p.bitmap[v >> 5], 1u << (v & 31));
+            t.claims += 1;
+            sh.claimed = 1;
+            st[0] = s0;
+            dg[0] = e0 - s0;
+            if (dg[0] >= p.large_min) lm = 1;
+            else if (dg[0] > 0) loc = 1;
+        }
+        if (__any_sync(kFull, lm)) push_large<PAR>(p, lv, lm, st, dg, vv);
+        push_local<PAR>(p, lv, loc, st, dg, vv);
+    }
+}
+
 // Per-warp state that outlives one BFS within a launch: the parity of each
 // of the warp's two mbarriers, and whether a bulk copy ever failed to land.
 struct WarpState {
@@ -987,6 +1051,9 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
     int cur = 0;
     int L = 0;
     Tally t{0u, 0u};
+    long long explored = 0;  // degree sum of the vertices visited so far (direction switch)
+    bool bottom_up = false;
+    int prev_pushed = 0;
 
     bool ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[0], sh.in, false);
 
@@ -1028,11 +1095,23 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         // where it scans fewer edges than one 4-edge round per lane of the
         // grid; 2 = decide per level
         lv.probe = p.probe_first == 2 ? (sh.in[4] >= 128 * nwarps ? 1 : 0) : p.probe_first;
+        // direction (Beamer, Asanovic and Patterson, SC 2012): go bottom-up when
+        // the frontier's edges exceed 1/14 of the edges of unvisited vertices,
+        // back to top-down once the frontier falls below n/24 and shrinks.
+        // Every block sees the same counters, so all decide alike.
+        explored += sh.in[4];
+        if (p.direction) {
+            const long long unexplored = (long long)p.e - explored;
+            if (!bottom_up && 14LL * sh.in[4] > unexplored) bottom_up = true;
+            else if (bottom_up && 24LL * pushed < (long long)p.n && pushed < prev_pushed) bottom_up = false;
+        }
+        prev_pushed = pushed;
+        lv.bottom_up = bottom_up ? 1 : 0;
         // probe levels consult the shared hot-vertex cache, refreshed here from
         // the global bitmap (everything visited before this level) and added
         // to during the level as this block meets visited vertices
         lv.hot = 0u;
-        if (lv.probe && p.hot_words > 0) {
+        if (lv.probe && !lv.bottom_up && p.hot_words > 0) {
             lv.hot = 32u * (unsigned)p.hot_words;
             const uint4* src4 = reinterpret_cast<const uint4*>(p.bitmap);
             uint4* dst4 = reinterpret_cast<uint4*>(hot_cache());
@@ -1043,157 +1122,167 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             ctl->trace_edges[L] = sh.in[4];
             ctl->trace_ovf[L] = n_ovf;
             ctl->trace_pieces[L] = total_pieces;
-            ctl->trace_probe[L] = lv.probe;
+            ctl->trace_probe[L] = lv.bottom_up ? 2 : lv.probe;
+        }
+        if (lv.bottom_up && grank == 0 && tid == 0) {
+            // E_R stays the degree sum of reached vertices: a bottom-up level
+            // does not scan the frontier's lists, so count them here
+            atomicAdd(&ctl->stats.edges, (unsigned long long)(unsigned)sh.in[4]);
         }
 
-        // (1) this block's own queue from the previous level, 32 entries per grab
-        {
-            const int nloc = sh.cnt_cur;
-            const int* qc = reinterpret_cast<const int*>(dfq_smem) + cur * 3 * p.local_cap;
-            while (true) {
-                int j = 0;
-                if (lane == 0) j = atomicAdd(&sh.local_grab, 32);
-                j = __shfl_sync(kFull, j, 0);
-                if (j >= nloc) break;
-                const int i = j + lane;
-                const bool has = i < nloc;
-                warp_process<PAR>(p, lv, t, ring, wl, has, has ? qc[i] : 0, has ? qc[p.local_cap + i] : 0,
-                                  (PAR && has) ? qc[2 * p.local_cap + i] : 0);
+        if (lv.bottom_up) {
+            // the frontier is read from the levels; this level's queues are not expanded
+            bottom_up_level<PAR>(p, lv, t, gwarp, nwarps);
+        } else {
+            // (1) this block's own queue from the previous level, 32 entries per grab
+            {
+                const int nloc = sh.cnt_cur;
+                const int* qc = reinterpret_cast<const int*>(dfq_smem) + cur * 3 * p.local_cap;
+                while (true) {
+                    int j = 0;
+                    if (lane == 0) j = atomicAdd(&sh.local_grab, 32);
+                    j = __shfl_sync(kFull, j, 0);
+                    if (j >= nloc) break;
+                    const int i = j + lane;
+                    const bool has = i < nloc;
+                    warp_process<PAR>(p, lv, t, ring, wl, has, has ? qc[i] : 0, has ? qc[p.local_cap + i] : 0,
+                                      (PAR && has) ? qc[2 * p.local_cap + i] : 0);
+                }
             }
-        }
 
-        // (2) large pieces: each warp pulls pieces and double-buffers their
-        //     bulk copies into its own shared-memory buffers.  Schedule: when
-        //     there are no more pieces than warps each piece goes to one warp;
-        //     otherwise the first 3/4 go round-robin and the rest are pulled
-        //     from a counter
-        if (total_pieces > 0 && !warp_failed) {
-            const int2* pin = p.piece[in];
-            const int* pvin = p.piece_v[in];
-            const int p_static = total_pieces <= nwarps ? total_pieces : total_pieces - total_pieces / 4;
-            // lane 0 runs a pipeline one piece deep in each stage: while piece
-            // k is expanded, piece k+1's copy is in flight, piece k+2's range
-            // is being loaded and piece k+3's index has been taken, so no
-            // dependent load or atomic sits between two pieces.  The next
-            // static index lives in the warp's gather scratch (unused while
-            // pieces are expanded).
-            int* pq = wl;
-            auto grab = [&]() -> int {  // lane 0: next piece index (total_pieces: none)
-                const int sn = pq[0];
-                if (sn < p_static) { pq[0] = sn + nwarps; return sn; }
-                if (p_static < total_pieces) return p_static + atomicAdd(&cin->large_grab, 1);
-                return total_pieces;
-            };
-            auto desc = [&](int g, int2& d, int& u) {  // lane 0: piece g's range (empty: none)
-                d = make_int2(0, 0);
-                u = 0;
-                if (g < total_pieces) {
-                    d = __ldcg(pin + g);
-                    if (PAR) u = __ldcg(pvin + g);
-                }
-            };
-            auto issue = [&](const int2& d, int b) {  // lane 0: stage piece d into buffer b
-                if (p.use_tma && d.y > d.x) {
-                    const int a0 = d.x & ~3, a1 = (d.y + 3) & ~3;
-                    const unsigned bytes = (unsigned)(a1 - a0) * 4u;
-                    mbar_arrive_expect_tx(&wbar[b], bytes);
-                    tma_load_1d(wbuf0 + b * (P + 16), p.cols + a0, bytes, &wbar[b]);
-                }
-            };
-            int2 dc = make_int2(0, 0), dn = dc;
-            int uc = 0, un = 0, gn = total_pieces;
-            if (lane == 0) {
-                pq[0] = gwarp;
-                desc(grab(), dc, uc);
-                issue(dc, 0);
-                desc(grab(), dn, un);
-                gn = grab();
-            }
-            int cb = 0;
-            while (true) {
-                const int lo = __shfl_sync(kFull, dc.x, 0), hi = __shfl_sync(kFull, dc.y, 0);
-                if (hi <= lo) break;
-                const int par0 = PAR ? __shfl_sync(kFull, uc, 0) : 0;
+            // (2) large pieces: each warp pulls pieces and double-buffers their
+            //     bulk copies into its own shared-memory buffers.  Schedule: when
+            //     there are no more pieces than warps each piece goes to one warp;
+            //     otherwise the first 3/4 go round-robin and the rest are pulled
+            //     from a counter
+            if (total_pieces > 0 && !warp_failed) {
+                const int2* pin = p.piece[in];
+                const int* pvin = p.piece_v[in];
+                const int p_static = total_pieces <= nwarps ? total_pieces : total_pieces - total_pieces / 4;
+                // lane 0 runs a pipeline one piece deep in each stage: while piece
+                // k is expanded, piece k+1's copy is in flight, piece k+2's range
+                // is being loaded and piece k+3's index has been taken, so no
+                // dependent load or atomic sits between two pieces.  The next
+                // static index lives in the warp's gather scratch (unused while
+                // pieces are expanded).
+                int* pq = wl;
+                auto grab = [&]() -> int {  // lane 0: next piece index (total_pieces: none)
+                    const int sn = pq[0];
+                    if (sn < p_static) { pq[0] = sn + nwarps; return sn; }
+                    if (p_static < total_pieces) return p_static + atomicAdd(&cin->large_grab, 1);
+                    return total_pieces;
+                };
+                auto desc = [&](int g, int2& d, int& u) {  // lane 0: piece g's range (empty: none)
+                    d = make_int2(0, 0);
+                    u = 0;
+                    if (g < total_pieces) {
+                        d = __ldcg(pin + g);
+                        if (PAR) u = __ldcg(pvin + g);
+                    }
+                };
+                auto issue = [&](const int2& d, int b) {  // lane 0: stage piece d into buffer b
+                    if (p.use_tma && d.y > d.x) {
+                        const int a0 = d.x & ~3, a1 = (d.y + 3) & ~3;
+                        const unsigned bytes = (unsigned)(a1 - a0) * 4u;
+                        mbar_arrive_expect_tx(&wbar[b], bytes);
+                        tma_load_1d(wbuf0 + b * (P + 16), p.cols + a0, bytes, &wbar[b]);
+                    }
+                };
+                int2 dc = make_int2(0, 0), dn = dc;
+                int uc = 0, un = 0, gn = total_pieces;
                 if (lane == 0) {
-                    issue(dn, cb ^ 1);
-                    dc = dn;
-                    uc = un;
-                    desc(gn, dn, un);
+                    pq[0] = gwarp;
+                    desc(grab(), dc, uc);
+                    issue(dc, 0);
+                    desc(grab(), dn, un);
                     gn = grab();
                 }
-                if (p.use_tma) {
-                    const bool landed = mbar_wait_bounded(&wbar[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
-                    if (__any_sync(kFull, !landed)) {
-                        // never expand a buffer whose copy did not land: record the
-                        // error, give this warp's copies one more bounded wait, stop
-                        if (lane == 0) {
-                            set_error(ctl, kErrTmaTimeout, (int)blockIdx.x, lo);
-                            mbar_wait_bounded(&wbar[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
-                            if (dc.y > dc.x)
-                                mbar_wait_bounded(&wbar[cb ^ 1], (phase_bits >> (cb ^ 1)) & 1u, p.timeout_ns);
-                        }
-                        warp_failed = true;
-                        break;
+                int cb = 0;
+                while (true) {
+                    const int lo = __shfl_sync(kFull, dc.x, 0), hi = __shfl_sync(kFull, dc.y, 0);
+                    if (hi <= lo) break;
+                    const int par0 = PAR ? __shfl_sync(kFull, uc, 0) : 0;
+                    if (lane == 0) {
+                        issue(dn, cb ^ 1);
+                        dc = dn;
+                        uc = un;
+                        desc(gn, dn, un);
+                        gn = grab();
                     }
-                    phase_bits ^= 1u << cb;
-                    const int* buf = wbuf0 + cb * (P + 16);
-                    const int a0 = lo & ~3, off = lo - a0, tw = hi - a0;
-                    if (lv.probe) {
-                        probe_piece<PAR>(p, lv, t, ring, buf, off, tw, par0);
-                    } else {
-                        const int par[4] = {par0, par0, par0, par0};
-                        for (int base = 0; base < tw; base += 128) {
-                            const int w4 = base + 4 * lane;
-                            int4 x = make_int4(0, 0, 0, 0);
-                            unsigned vm = 0;
-                            if (w4 < tw) {
-                                x = *reinterpret_cast<const int4*>(buf + w4);
-#pragma unroll
-                                for (int j = 0; j < 4; ++j)
-                                    if (w4 + j >= off && w4 + j < tw) vm |= 1u << j;
+                    if (p.use_tma) {
+                        const bool landed = mbar_wait_bounded(&wbar[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
+                        if (__any_sync(kFull, !landed)) {
+                            // never expand a buffer whose copy did not land: record the
+                            // error, give this warp's copies one more bounded wait, stop
+                            if (lane == 0) {
+                                set_error(ctl, kErrTmaTimeout, (int)blockIdx.x, lo);
+                                mbar_wait_bounded(&wbar[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
+                                if (dc.y > dc.x)
+                                    mbar_wait_bounded(&wbar[cb ^ 1], (phase_bits >> (cb ^ 1)) & 1u, p.timeout_ns);
                             }
-                            const int v[4] = {x.x, x.y, x.z, x.w};
-                            scan4<PAR>(p, lv, t, ring, v, vm, par);
+                            warp_failed = true;
+                            break;
                         }
+                        phase_bits ^= 1u << cb;
+                        const int* buf = wbuf0 + cb * (P + 16);
+                        const int a0 = lo & ~3, off = lo - a0, tw = hi - a0;
+                        if (lv.probe) {
+                            probe_piece<PAR>(p, lv, t, ring, buf, off, tw, par0);
+                        } else {
+                            const int par[4] = {par0, par0, par0, par0};
+                            for (int base = 0; base < tw; base += 128) {
+                                const int w4 = base + 4 * lane;
+                                int4 x = make_int4(0, 0, 0, 0);
+                                unsigned vm = 0;
+                                if (w4 < tw) {
+                                    x = *reinterpret_cast<const int4*>(buf + w4);
+    #pragma unroll
+                                    for (int j = 0; j < 4; ++j)
+                                        if (w4 + j >= off && w4 + j < tw) vm |= 1u << j;
+                                }
+                                const int v[4] = {x.x, x.y, x.z, x.w};
+                                scan4<PAR>(p, lv, t, ring, v, vm, par);
+                            }
+                        }
+                    } else {
+                        warp_expand<PAR>(p, lv, t, ring, lo, hi - lo, par0);
                     }
-                } else {
-                    warp_expand<PAR>(p, lv, t, ring, lo, hi - lo, par0);
+                    __syncwarp();
+                    cb ^= 1;
                 }
-                __syncwarp();
-                cb ^= 1;
             }
-        }
 
-        // (3) global overflow queue in 32-entry chunks, same schedule as the
-        //     pieces; the next chunk index is fetched before the current one
-        //     is expanded
-        if (n_ovf > 0) {
-            const int2* ovf_in = p.ovf[in];
-            const int* ovfv_in = p.ovfv[in];
-            const int n_chunks = (n_ovf + 31) >> 5;
-            const int c_static = n_chunks <= nwarps ? n_chunks : n_chunks - (n_chunks >> 2);
-            int s_next = gwarp;
-            auto next_chunk = [&]() -> int {  // lane 0 only
-                if (s_next < c_static) { const int ci = s_next; s_next += nwarps; return ci; }
-                if (c_static < n_chunks) return c_static + atomicAdd(&cin->ovf_grab, 1);
-                return n_chunks;
-            };
-            int nxt = 0;
-            if (lane == 0) nxt = next_chunk();
-            while (true) {
-                const int ci = __shfl_sync(kFull, nxt, 0);
-                if (ci >= n_chunks) break;
-                const int c0 = ci << 5;
+            // (3) global overflow queue in 32-entry chunks, same schedule as the
+            //     pieces; the next chunk index is fetched before the current one
+            //     is expanded
+            if (n_ovf > 0) {
+                const int2* ovf_in = p.ovf[in];
+                const int* ovfv_in = p.ovfv[in];
+                const int n_chunks = (n_ovf + 31) >> 5;
+                const int c_static = n_chunks <= nwarps ? n_chunks : n_chunks - (n_chunks >> 2);
+                int s_next = gwarp;
+                auto next_chunk = [&]() -> int {  // lane 0 only
+                    if (s_next < c_static) { const int ci = s_next; s_next += nwarps; return ci; }
+                    if (c_static < n_chunks) return c_static + atomicAdd(&cin->ovf_grab, 1);
+                    return n_chunks;
+                };
+                int nxt = 0;
                 if (lane == 0) nxt = next_chunk();
-                const int i = c0 + lane;
-                const bool has = i < n_ovf;
-                int2 x = make_int2(0, 0);
-                int u = 0;
-                if (has) {
-                    x = __ldcg(ovf_in + i);
-                    if (PAR) u = __ldcg(ovfv_in + i);
+                while (true) {
+                    const int ci = __shfl_sync(kFull, nxt, 0);
+                    if (ci >= n_chunks) break;
+                    const int c0 = ci << 5;
+                    if (lane == 0) nxt = next_chunk();
+                    const int i = c0 + lane;
+                    const bool has = i < n_ovf;
+                    int2 x = make_int2(0, 0);
+                    int u = 0;
+                    if (has) {
+                        x = __ldcg(ovf_in + i);
+                        if (PAR) u = __ldcg(ovfv_in + i);
+                    }
+                    warp_process<PAR>(p, lv, t, ring, wl, has, x.x, x.y, u);
                 }
-                warp_process<PAR>(p, lv, t, ring, wl, has, x.x, x.y, u);
             }
         }
         // claim whatever candidates this warp still holds

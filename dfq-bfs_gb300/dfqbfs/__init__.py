@@ -66,7 +66,8 @@ class Opts(C.Structure):
                 ("probe_first", C.c_int32), ("l2_persist", C.c_int32),
                 ("use_tma", C.c_int32), ("timeout_ms", C.c_int32),
                 ("wide_min_edges", C.c_int32), ("wide_min_degree", C.c_int32),
-                ("hot_cache", C.c_int32), ("vertex_order", C.c_int32), ("profile", C.c_int32)]
+                ("hot_cache", C.c_int32), ("vertex_order", C.c_int32), ("profile", C.c_int32),
+                ("direction", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

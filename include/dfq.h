@@ -156,6 +156,13 @@ typedef struct dfq_opts {
                                    in the input ids. */
     int32_t profile;            /* 1: also record when each block finished each level (the
                                    spread and barrier times of dfq_bfs_last_levels) */
+    int32_t direction;          /* 0: top-down levels only (the reference's algorithm);
+                                   1: direction-optimising - levels whose frontier holds many
+                                   edges run bottom-up (each unvisited vertex looks for a parent
+                                   among its neighbours).  Needs an undirected graph: give 1 to
+                                   dfq_graph_create, which checks that every row is sorted and
+                                   every edge u->v has its v->u (else DFQ_EINVAL).  Same levels;
+                                   parents may differ (still a BFS tree); E_R still reported. */
 } dfq_opts;
 
 typedef struct dfq_stats {
@@ -237,7 +244,7 @@ typedef struct dfq_level_info {
     int32_t edges;          /* their degree sum: adjacency entries the level scans */
     int32_t overflow;       /* entries read from the global overflow queue */
     int32_t pieces;         /* large-list pieces */
-    int32_t probe;          /* 1: probe-then-claim level, 0: claim at once */
+    int32_t probe;          /* 1: probe-then-claim level, 0: claim at once, 2: bottom-up */
     int32_t pad;
 } dfq_level_info;
 int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels);

@@ -213,6 +213,40 @@ def test_hub_first_auto_and_device_input():
     run_and_check(grid, 0, opts(vertex_order=0))
 
 
+@pytest.mark.parametrize("order", [0, 1])
+def test_direction_optimizing(order):
+    """Direction-optimising levels give the oracle's levels, a valid BFS tree
+    and E_R; RMAT's large levels do run bottom-up."""
+    g = d.gen_rmat(17, 16, seed=31)
+    with d.Graph(g, opts=opts(direction=1, vertex_order=order)) as dg:
+        for s in g.pick_sources(4, seed=31):
+            run_and_check(g, int(s), graph=dg)
+        prof = dg.last_levels(64)
+        assert any(r["probe"] == 2 for r in prof)          # some level went bottom-up
+        assert prof[1]["probe"] != 2 or prof[0]["probe"] != 2  # not every level
+    grid, _ = d.gen_grid(200, 0.02, seed=31)
+    with d.Graph(grid, opts=opts(direction=1)) as dg:
+        run_and_check(grid, 0, graph=dg)
+    # a disconnected undirected graph: unreached vertices stay -1
+    two = d.from_edges([0, 1, 5, 6], [1, 2, 6, 7], 9, d.CSR_SYMMETRIZE | d.CSR_DEDUP)
+    with d.Graph(two, opts=opts(direction=1)) as dg:
+        run_and_check(two, 0, graph=dg)
+
+
+def test_direction_optimizing_needs_undirected():
+    directed = d.gen_zipf_geometric(5000, 4.7, 2.1, seed=3)
+    with pytest.raises(d.DfqError) as e:
+        d.Graph(directed, opts=opts(direction=1))
+    assert e.value.name == "EINVAL"
+    g = d.gen_rmat(10, 8, seed=3)
+    with d.Graph(g) as dg:  # created top-down only: asking for bottom-up later is refused
+        o = dg.opts()
+        o.direction = 1
+        dg.set_opts(o)
+        with pytest.raises(d.DfqError):
+            dg.bfs(0)
+
+
 def test_repeated_runs_identical():
     g = d.gen_rmat(15, 16, seed=8)
     src = int(g.pick_sources(1, seed=8)[0])
