@@ -542,22 +542,48 @@ __device__ __forceinline__ void push_large(const Params& p, const Lv& lv, unsign
         if (base + totp > (unsigned)p.piece_cap) set_error(p.ctl, kErrQueueCap, (int)base, (int)totp);
     }
     base = __shfl_sync(kFull, base, 0);
-    if (!lm) return;
     // pieces past the capacity are dropped (the error is recorded above);
     // readers clamp the piece count to the capacity, so every piece read
     // was written at this level
     unsigned poff = base + (unsigned)(incl - npl);
     int2* pc = lv.out ? p.piece[1] : p.piece[0];
     int* pv = lv.out ? p.piece_v[1] : p.piece_v[0];
+    // lists of a few pieces: each lane writes its own; longer lists (hubs,
+    // up to thousands of pieces) are written by the whole warp in turn
+    constexpr int kOwn = 4;
+    unsigned big = 0;
+    unsigned boff[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         if (!(lm >> j & 1)) continue;
-        const int a0 = st[j] & ~3, e1 = st[j] + dg[j], np = pieces_of(st[j], dg[j], P);
-        for (int i = 0; i < np && poff + (unsigned)i < (unsigned)p.piece_cap; ++i) {
-            pc[poff + i] = make_int2(max(st[j], a0 + i * P), min(e1, a0 + (i + 1) * P));
-            if (PAR) pv[poff + i] = v[j];
+        const int np = pieces_of(st[j], dg[j], P);
+        boff[j] = poff;
+        if (np > kOwn) {
+            big |= 1u << j;
+        } else {
+            const int a0 = st[j] & ~3, e1 = st[j] + dg[j];
+            for (int i = 0; i < np && poff + (unsigned)i < (unsigned)p.piece_cap; ++i) {
+                pc[poff + i] = make_int2(max(st[j], a0 + i * P), min(e1, a0 + (i + 1) * P));
+                if (PAR) pv[poff + i] = v[j];
+            }
         }
         poff += (unsigned)np;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        unsigned m = __ballot_sync(kFull, big >> j & 1);
+        while (m) {
+            const int i = __ffs(m) - 1;
+            m &= m - 1;
+            const int s0 = __shfl_sync(kFull, st[j], i), d0 = __shfl_sync(kFull, dg[j], i);
+            const int v0 = __shfl_sync(kFull, v[j], i);
+            const unsigned o0 = __shfl_sync(kFull, boff[j], i);
+            const int a0 = s0 & ~3, e1 = s0 + d0, np = pieces_of(s0, d0, P);
+            for (int k = lane; k < np && o0 + (unsigned)k < (unsigned)p.piece_cap; k += 32) {
+                pc[o0 + k] = make_int2(max(s0, a0 + k * P), min(e1, a0 + (k + 1) * P));
+                if (PAR) pv[o0 + k] = v0;
+            }
+        }
     }
 }
 
