@@ -52,11 +52,10 @@ enum : int { kErrNone = 0, kErrBarrierTimeout = 1, kErrTmaTimeout = 2, kErrQueue
 // counters and the two consumer cursors sit on separate 128-byte lines so
 // atomics on one do not queue behind atomics on another.
 struct alignas(128) LevelCtr {
-    int ovf_count;                  // entries in the global overflow queue
+    unsigned long long ovf_pieces;  // (global overflow queue entries << 32) | large-list pieces
     int pushed;                     // frontier entries (local + overflow + large)
-    unsigned long long large_pack;  // (large entries << 32) | pieces
     int pushed_edges;               // sum of the degrees of those entries
-    int pad0[27];
+    int pad0[28];
     int ovf_grab;                   // chunk cursor over the overflow queue
     int pad1[31];
     int large_grab;                 // piece cursor over the large queue
@@ -280,14 +279,13 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
             // the status word and the counters in one round of loads
             const int st = *(volatile int*)&ctl->status;
             const int pushed = __ldcg(&next->pushed);
-            const int ovf = __ldcg(&next->ovf_count);
-            const unsigned long long lp = __ldcg(&next->large_pack);
+            const unsigned long long op = __ldcg(&next->ovf_pieces);
             const int edges = __ldcg(&next->pushed_edges);
             ok = st == 0;
             s_in[0] = pushed;
-            s_in[1] = ovf;
-            s_in[2] = (int)(lp >> 32);
-            s_in[3] = (int)(unsigned)lp;
+            s_in[1] = (int)(op >> 32);
+            s_in[2] = 0;
+            s_in[3] = (int)(unsigned)op;
             s_in[4] = edges;
         }
         *s_flag = ok;
@@ -316,10 +314,10 @@ __device__ __forceinline__ bool group_barrier(Control* ctl, int gsize, unsigned&
         *s_flag = ok;
         if (ok) {
             s_in[0] = __ldcg(&next->pushed);
-            s_in[1] = __ldcg(&next->ovf_count);
-            const unsigned long long lp = __ldcg(&next->large_pack);
-            s_in[2] = (int)(lp >> 32);
-            s_in[3] = (int)(unsigned)lp;
+            const unsigned long long op = __ldcg(&next->ovf_pieces);
+            s_in[1] = (int)(op >> 32);
+            s_in[2] = 0;
+            s_in[3] = (int)(unsigned)op;
             s_in[4] = __ldcg(&next->pushed_edges);
         }
     }
@@ -427,49 +425,92 @@ struct Ring {
     int n;
 };
 
-// Push up to four claimed vertices per lane into the block's next local
-// queue, all-or-nothing per warp against its entry limit and edge budget;
-// a batch that does not fit goes to the global overflow queue.
-// Warp-collective: every lane calls it (loc == 0 if it has nothing).
+// Pieces of a list [st, st + dg) cut at multiples of the piece size counted
+// from its 16-byte aligned floor a0 = st & ~3: every piece's staged span is
+// at most piece_edges entries and starts aligned.
+__device__ __forceinline__ int pieces_of(int st, int dg, int P) { return (st + dg - (st & ~3) + P - 1) / P; }
+
+// Push this warp's claimed vertices (bit j of loc / lm: entry j of this lane
+// is small / large).  Small entries go to the block's next local queue,
+// all-or-nothing per warp against its entry limit and edge budget, else to
+// the global overflow queue; large entries become pieces.  The overflow
+// slots and the pieces of the whole warp come from ONE 64-bit atomic on the
+// level's (overflow entries << 32 | pieces) word, handed out in lane order:
+// levels that claim hundreds of thousands of vertices otherwise queue behind
+// same-address atomics.  Warp-collective.
 template <bool PAR>
-__device__ __forceinline__ void push_local(const Params& p, const Lv& lv, unsigned loc, const int (&st)[4],
-                                           const int (&dg)[4], const int (&v)[4]) {
+__device__ __forceinline__ void push_claims(const Params& p, const Lv& lv, unsigned loc, unsigned lm,
+                                            const int (&st)[4], const int (&dg)[4], const int (&v)[4]) {
+    if (!__any_sync(kFull, loc | lm)) return;
     const int lane = threadIdx.x & 31;
-    const int cnt = __popc(loc);
-    int dsum = 0;
+    const int P = p.piece_edges;
+    int cnt = __popc(loc), npl = 0;
+    unsigned dsum = 0, dlarge = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
-        if (loc >> j & 1) dsum += dg[j];
-    int incl = cnt;
+    for (int j = 0; j < 4; ++j) {
+        if (loc >> j & 1) dsum += (unsigned)dg[j];
+        if (lm >> j & 1) {
+            npl += pieces_of(st[j], dg[j], P);
+            dlarge += (unsigned)dg[j];
+        }
+    }
+    // one scan for both prefix sums: small entries (< 2^7 per warp) in the
+    // high bits, pieces (< 2^24 per warp) in the low bits
+    int incl = (cnt << 24) | npl;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += t;
+        const int tt = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += tt;
     }
-    const int tot = __shfl_sync(kFull, incl, 31);
-    if (tot == 0) return;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(kFull, dsum, o);
+    const int tot_both = __shfl_sync(kFull, incl, 31);
+    const int tot = (int)((unsigned)tot_both >> 24), totp = tot_both & 0xffffff;
+    const int tsum = (int)__reduce_add_sync(kFull, dsum);
     int base = -1, gbase = 0;
+    unsigned pbase = 0;
     if (lane == 0) {
-        unsigned long long old = *(volatile unsigned long long*)&sh.local_pack;
-        while (true) {
-            const unsigned n_ent = (unsigned)(old >> 32), n_deg = (unsigned)old;
-            if (n_ent + (unsigned)tot > (unsigned)lv.cap || n_deg + (unsigned)dsum > (unsigned)p.local_budget) break;
-            const unsigned long long want =
-                ((unsigned long long)(n_ent + tot) << 32) | (unsigned long long)(n_deg + (unsigned)dsum);
-            const unsigned long long seen = atomicCAS(&sh.local_pack, old, want);
-            if (seen == old) { base = (int)n_ent; break; }
-            old = seen;
+        if (tot > 0) {
+            unsigned long long old = *(volatile unsigned long long*)&sh.local_pack;
+            while (true) {
+                const unsigned n_ent = (unsigned)(old >> 32), n_deg = (unsigned)old;
+                if (n_ent + (unsigned)tot > (unsigned)lv.cap || n_deg + (unsigned)tsum > (unsigned)p.local_budget)
+                    break;
+                const unsigned long long want =
+                    ((unsigned long long)(n_ent + tot) << 32) | (unsigned long long)(n_deg + (unsigned)tsum);
+                const unsigned long long seen = atomicCAS(&sh.local_pack, old, want);
+                if (seen == old) { base = (int)n_ent; break; }
+                old = seen;
+            }
         }
-        if (base < 0) {
-            gbase = atomicAdd(&p.ctl->lv[lv.cslot].ovf_count, tot);
-            atomicAdd(&sh.ovf_pushed, tot);
-            atomicAdd(&sh.ovf_edges, dsum);
+        const int to_ovf = (tot > 0 && base < 0) ? tot : 0;
+        if (to_ovf || totp) {
+            const unsigned long long old = atomicAdd(&p.ctl->lv[lv.cslot].ovf_pieces,
+                                                     ((unsigned long long)to_ovf << 32) | (unsigned)totp);
+            gbase = (int)(old >> 32);
+            pbase = (unsigned)old;
+        }
+        if (to_ovf) {
+            atomicAdd(&sh.ovf_pushed, to_ovf);
+            atomicAdd(&sh.ovf_edges, tsum);
+        }
+        if (totp) {
+            atomicAdd(&sh.large_pieces, totp);
+            if (pbase + (unsigned)totp > (unsigned)p.piece_cap) set_error(p.ctl, kErrQueueCap, (int)pbase, totp);
+        }
+    }
+    if (totp) {  // warp-uniform: entry and edge tallies of the large claims
+        const unsigned totc = __reduce_add_sync(kFull, (unsigned)__popc(lm));
+        const unsigned totd = __reduce_add_sync(kFull, dlarge);
+        if (lane == 0) {
+            atomicAdd(&sh.large_pushed, (int)totc);
+            atomicAdd(&sh.large_edges, (int)totd);
         }
     }
     base = __shfl_sync(kFull, base, 0);
-    int pos = incl - cnt;
+    gbase = __shfl_sync(kFull, gbase, 0);
+    pbase = __shfl_sync(kFull, pbase, 0);
+
+    // small entries
+    int pos = (int)((unsigned)incl >> 24) - cnt;
     if (base >= 0) {
         int* qs = reinterpret_cast<int*>(dfq_smem) + lv.qn * 3 * p.local_cap;
 #pragma unroll
@@ -481,8 +522,7 @@ __device__ __forceinline__ void push_local(const Params& p, const Lv& lv, unsign
                 ++pos;
             }
         }
-    } else {
-        gbase = __shfl_sync(kFull, gbase, 0);
+    } else if (tot > 0) {
         int2* ovf = lv.out ? p.ovf[1] : p.ovf[0];
         int* ovfv = lv.out ? p.ovfv[1] : p.ovfv[0];
 #pragma unroll
@@ -499,57 +539,15 @@ __device__ __forceinline__ void push_local(const Params& p, const Lv& lv, unsign
             }
         }
     }
-}
+    if (!totp) return;
 
-// Push this warp's claimed large-degree vertices (bit j of lm: entry j of
-// this lane) with one atomic for the whole warp; slots and piece ranges are
-// handed out in lane order.  A list [st, st + dg) is cut at multiples of the
-// piece size counted from its 16-byte aligned floor a0 = st & ~3, so every
-// piece's staged span is at most piece_edges entries and starts aligned.
-// Warp-collective.
-__device__ __forceinline__ int pieces_of(int st, int dg, int P) { return (st + dg - (st & ~3) + P - 1) / P; }
-
-template <bool PAR>
-__device__ __forceinline__ void push_large(const Params& p, const Lv& lv, unsigned lm, const int (&st)[4],
-                                           const int (&dg)[4], const int (&v)[4]) {
-    const int lane = threadIdx.x & 31;
-    const int P = p.piece_edges;
-    int npl = 0;
-    unsigned dsum = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-        if (lm >> j & 1) {
-            npl += pieces_of(st[j], dg[j], P);
-            dsum += (unsigned)dg[j];
-        }
-    int incl = npl;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int tt = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += tt;
-    }
-    const unsigned totp = (unsigned)__shfl_sync(kFull, incl, 31);
-    const unsigned totc = __reduce_add_sync(kFull, (unsigned)__popc(lm));
-    const unsigned totd = __reduce_add_sync(kFull, dsum);
-    unsigned base = 0;
-    if (lane == 0) {
-        const unsigned long long old =
-            atomicAdd(&p.ctl->lv[lv.cslot].large_pack, ((unsigned long long)totc << 32) | totp);
-        base = (unsigned)old;
-        atomicAdd(&sh.large_pushed, (int)totc);
-        atomicAdd(&sh.large_pieces, (int)totp);
-        atomicAdd(&sh.large_edges, (int)totd);
-        if (base + totp > (unsigned)p.piece_cap) set_error(p.ctl, kErrQueueCap, (int)base, (int)totp);
-    }
-    base = __shfl_sync(kFull, base, 0);
-    // pieces past the capacity are dropped (the error is recorded above);
-    // readers clamp the piece count to the capacity, so every piece read
-    // was written at this level
-    unsigned poff = base + (unsigned)(incl - npl);
+    // pieces (dropped past the capacity, where the error is recorded above;
+    // readers clamp the piece count to the capacity, so every piece read was
+    // written at this level).  Lists of a few pieces: each lane writes its
+    // own; longer lists (hubs, up to thousands of pieces) the whole warp.
+    unsigned poff = pbase + (unsigned)((incl & 0xffffff) - npl);
     int2* pc = lv.out ? p.piece[1] : p.piece[0];
     int* pv = lv.out ? p.piece_v[1] : p.piece_v[0];
-    // lists of a few pieces: each lane writes its own; longer lists (hubs,
-    // up to thousands of pieces) are written by the whole warp in turn
     constexpr int kOwn = 4;
     unsigned big = 0;
     unsigned boff[4] = {0u, 0u, 0u, 0u};
@@ -587,132 +585,94 @@ __device__ __forceinline__ void push_large(const Params& p, const Lv& lv, unsign
     }
 }
 
-// Scan up to four neighbours per lane: probe, claim, record, push.
-// Warp-collective (calls push_local).
+// Claim up to four candidates per lane (bit j of vm: v[j]), with each one's
+// row bounds loaded alongside its atomicOr; record and push what this warp
+// wins.  On levels that do not probe, the winners' rows are also prefetched
+// into L2 for the next level.  Warp-collective.
 template <bool PAR>
-__device__ __forceinline__ void visit4(const Params& p, const Lv& lv, Tally& t, const int (&v)[4], unsigned vmask,
+__device__ __forceinline__ void claim4(const Params& p, const Lv& lv, Tally& t, const int (&v)[4], unsigned vm,
                                        const int (&par)[4]) {
-    unsigned claim = 0;
-    int so[4], eo[4];  // offsets[v], offsets[v+1]
-    if (!lv.probe) {
-        // small frontier: latency, not atomic traffic, bounds the level, so
-        // every candidate's row bounds are loaded alongside its atomicOr
+    int so[4], eo[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            so[j] = 0;
-            eo[j] = 0;
-            if (vmask >> j & 1) {
-                so[j] = __ldg(p.offsets + v[j]);
-                eo[j] = __ldg(p.offsets + v[j] + 1);
-            }
+    for (int j = 0; j < 4; ++j) {
+        so[j] = 0;
+        eo[j] = 0;
+        if (vm >> j & 1) {
+            so[j] = __ldg(p.offsets + v[j]);
+            eo[j] = __ldg(p.offsets + v[j] + 1);
         }
     }
-    if (vmask) {
-        unsigned w[4] = {0u, 0u, 0u, 0u};
-        if (lv.probe) {
+    unsigned won = 0;
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-                if (vmask >> j & 1) w[j] = p.bitmap[v[j] >> 5];
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const unsigned bit = 1u << (v[j] & 31);
-            if ((vmask >> j & 1) && !(w[j] & bit)) {
-                const unsigned old = atomicOr(&p.bitmap[v[j] >> 5], bit);
-                if (!(old & bit)) claim |= 1u << j;
-            }
-        }
-        t.edges += __popc(vmask);
+    for (int j = 0; j < 4; ++j) {
+        if (!(vm >> j & 1)) continue;
+        const unsigned bit = 1u << (v[j] & 31);
+        if (!(atomicOr(&p.bitmap[v[j] >> 5], bit) & bit)) won |= 1u << j;
+        hot_learn(lv, v[j]);  // visited now, whoever won
     }
     int st[4], dg[4];
-    unsigned loc = 0;
+    unsigned loc = 0, lm = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         st[j] = 0;
         dg[j] = 0;
-        if (claim >> j & 1) {
-            p.levels[v[j]] = lv.next;
-            if (PAR) p.parents[v[j]] = par[j];
-            if (lv.probe) {
-                st[j] = __ldg(p.offsets + v[j]);
-                dg[j] = __ldg(p.offsets + v[j] + 1) - st[j];
-            } else {
-                st[j] = so[j];
-                dg[j] = eo[j] - so[j];
-                // small frontier: pull the row this vertex will expand at the
-                // next level into L2 now, off the next level's critical path
-                if (dg[j] > 0) {
-                    prefetch_l2(p.cols + st[j]);
-                    if (dg[j] > 32) prefetch_l2(p.cols + st[j] + dg[j] - 1);
-                }
-            }
+        if (!(won >> j & 1)) continue;
+        p.levels[v[j]] = lv.next;
+        if (PAR) p.parents[v[j]] = par[j];
+        st[j] = so[j];
+        dg[j] = eo[j] - so[j];
+        if (!lv.probe && dg[j] > 0) {
+            // small frontier: pull the row this vertex expands at the next
+            // level into L2 now, off the next level's critical path
+            prefetch_l2(p.cols + st[j]);
+            if (dg[j] > 32) prefetch_l2(p.cols + st[j] + dg[j] - 1);
         }
+        if (dg[j] >= p.large_min) lm |= 1u << j;
+        else if (dg[j] > 0) loc |= 1u << j;
     }
-    unsigned lm = 0;
-    if (claim) {
-        t.claims += __popc(claim);
-        sh.claimed = 1;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            if (!(claim >> j & 1) || dg[j] == 0) continue;
-            if (dg[j] >= p.large_min) lm |= 1u << j;
-            else loc |= 1u << j;
-        }
-    }
-    if (__any_sync(kFull, lm)) push_large<PAR>(p, lv, lm, st, dg, v);
-    push_local<PAR>(p, lv, loc, st, dg, v);
-}
-
-// Claim one candidate per lane (has == false: none) and record / push what
-// it wins.  Warp-collective.
-template <bool PAR>
-__device__ __forceinline__ void claim1(const Params& p, const Lv& lv, Tally& t, bool has, int v, int par) {
-    bool won = false;
-    int so = 0, eo = 0;
-    if (has) {
-        // row bounds fetched alongside the claim: a candidate that passed the
-        // probe is usually still unvisited, so these loads are rarely wasted
-        so = __ldg(p.offsets + v);
-        eo = __ldg(p.offsets + v + 1);
-        const unsigned bit = 1u << (v & 31);
-        won = !(atomicOr(&p.bitmap[v >> 5], bit) & bit);
-        hot_learn(lv, v);  // visited now, whoever won
-    }
-    int st[4] = {0, 0, 0, 0}, dg[4] = {0, 0, 0, 0};
-    const int vv[4] = {v, 0, 0, 0};
-    unsigned loc = 0, lm = 0;
     if (won) {
-        p.levels[v] = lv.next;
-        if (PAR) p.parents[v] = par;
-        st[0] = so;
-        dg[0] = eo - so;
-        t.claims += 1;
+        t.claims += __popc(won);
         sh.claimed = 1;
-        if (dg[0] >= p.large_min) lm = 1;
-        else if (dg[0] > 0) loc = 1;
     }
-    if (__any_sync(kFull, lm)) push_large<PAR>(p, lv, lm, st, dg, vv);
-    push_local<PAR>(p, lv, loc, st, dg, vv);
+    push_claims<PAR>(p, lv, loc, lm, st, dg, v);
 }
 
-// Claim buffered candidates 32 at a time while at least 32 are waiting (or
-// until the ring is empty when `all`).  Warp-collective.
+// Levels that do not probe: claim the scanned neighbours at once.
+// Warp-collective.
+template <bool PAR>
+__device__ __forceinline__ void visit4(const Params& p, const Lv& lv, Tally& t, const int (&v)[4], unsigned vmask,
+                                       const int (&par)[4]) {
+    t.edges += __popc(vmask);
+    claim4<PAR>(p, lv, t, v, vmask, par);
+}
+
+// Claim buffered candidates 128 at a time (four per lane) while at least
+// 128 are waiting, or until the ring is empty when `all`.  Larger batches
+// mean fewer pushes, so fewer atomics on the level's counters.
+// Warp-collective.
 template <bool PAR>
 __device__ __forceinline__ void ring_drain(const Params& p, const Lv& lv, Tally& t, Ring& r, bool all) {
     const int lane = threadIdx.x & 31;
-    while (r.n >= 32 || (all && r.n > 0)) {
-        const int take = r.n < 32 ? r.n : 32;
-        const bool has = lane < take;
-        int v = 0, par = 0;
-        if (has) {
-            const int idx = (r.head + lane) & (kRing - 1);
-            v = r.v[idx];
-            if (PAR) par = r.v[kRing + idx];
+    while (r.n >= 128 || (all && r.n > 0)) {
+        const int take = r.n < 128 ? r.n : 128;
+        int v[4], par[4];
+        unsigned vm = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            v[j] = 0;
+            par[j] = 0;
+            const int k = j * 32 + lane;
+            if (k < take) {
+                const int idx = (r.head + k) & (kRing - 1);
+                v[j] = r.v[idx];
+                if (PAR) par[j] = r.v[kRing + idx];
+                vm |= 1u << j;
+            }
         }
         __syncwarp();
         r.head = (r.head + take) & (kRing - 1);
         r.n -= take;
-        claim1<PAR>(p, lv, t, has, v, par);
+        claim4<PAR>(p, lv, t, v, vm, par);
     }
 }
 
@@ -733,9 +693,9 @@ __device__ __forceinline__ unsigned hot_filter(const Lv& lv, const int (&v)[K], 
 
 // Probe levels: test up to four neighbours per lane against the visited
 // bitmap and append the unvisited ones to the warp's ring (prefix-sum
-// compaction); claims happen in full-warp batches in ring_drain.  The ring
-// holds < 32 entries between calls, so one call (<= 128 appends) never wraps
-// onto unclaimed entries.  Warp-collective.
+// compaction); claims happen in batches of 128 in ring_drain.  The ring
+// holds < 128 entries between calls, so one call (<= 128 appends) never
+// wraps onto unclaimed entries.  Warp-collective.
 template <bool PAR>
 __device__ __forceinline__ void probe4(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[4],
                                        unsigned vmask, const int (&par)[4]) {
@@ -778,8 +738,8 @@ __device__ __forceinline__ void probe4(const Params& p, const Lv& lv, Tally& t, 
 
 // Probe levels, eight neighbours per lane (all of one vertex, par0): the
 // eight bitmap loads are in flight together; candidates are appended in two
-// halves of at most 128 with a drain between, so the ring (< 32 entries
-// between calls) never holds more than 159.  One scan serves both halves
+// halves of at most 128 with a drain between, so the ring (< 128 entries
+// between calls) never holds more than 255.  One scan serves both halves
 // (counts packed in 16-bit fields).  Warp-collective.
 template <bool PAR>
 __device__ __forceinline__ void probe8(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[8],
@@ -989,8 +949,7 @@ __device__ __forceinline__ void bottom_up_level(const Params& p, const Lv& lv, T
             if (dg[0] >= p.large_min) lm = 1;
             else if (dg[0] > 0) loc = 1;
         }
-        if (__any_sync(kFull, lm)) push_large<PAR>(p, lv, lm, st, dg, vv);
-        push_local<PAR>(p, lv, loc, st, dg, vv);
+        push_claims<PAR>(p, lv, loc, lm, st, dg, vv);
     }
 }
 
@@ -1041,21 +1000,21 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             const int s0 = p.offsets[src], d = p.offsets[src + 1] - s0;
             if (d > 0) {
                 if (d >= p.large_min) {
-                    // the source's list in pieces, cut as push_large cuts lists
+                    // the source's list in pieces, cut as push_claims cuts lists
                     const int a0 = s0 & ~3, np = (s0 + d - a0 + P - 1) / P;
                     if (np <= p.piece_cap) {
                         for (int i = 0; i < np; ++i) {
                             p.piece[0][i] = make_int2(max(s0, a0 + i * P), min(s0 + d, a0 + (i + 1) * P));
                             if (PAR) p.piece_v[0][i] = src;
                         }
-                        ctl->lv[0].large_pack = (1ull << 32) | (unsigned)np;
+                        ctl->lv[0].ovf_pieces = (unsigned)np;
                     } else {
                         set_error(ctl, kErrQueueCap, np, p.piece_cap);
                     }
                 } else {
                     p.ovf[0][0] = make_int2(s0, d);
                     if (PAR) p.ovfv[0][0] = src;
-                    ctl->lv[0].ovf_count = 1;
+                    ctl->lv[0].ovf_pieces = 1ull << 32;
                 }
                 ctl->lv[0].pushed = 1;
                 ctl->lv[0].pushed_edges = d;
@@ -1093,12 +1052,12 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         LevelCtr* cin = &ctl->lv[L % 3];
         if (grank == 0 && tid == 0) {
             LevelCtr* cz = &ctl->lv[(L + 2) % 3];
-            cz->ovf_count = 0;
+
             cz->ovf_grab = 0;
             cz->large_grab = 0;
             cz->pushed = 0;
             cz->pushed_edges = 0;
-            cz->large_pack = 0ull;
+            cz->ovf_pieces = 0ull;
         }
         const int in = L & 1;
         // counts past a queue's capacity (recorded as an error when pushed)
