@@ -477,7 +477,7 @@ void dfq_opts_default(dfq_opts* o) {
     if (!o) return;
     o->block_threads = 512;
     o->blocks_per_sm = 0;
-    o->medium_min_degree = 32;
+    o->medium_min_degree = 64;
     o->large_min_degree = 256;
     o->local_queue_cap = 256;
     o->local_edge_budget = 8192;

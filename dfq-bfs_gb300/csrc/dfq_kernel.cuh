@@ -425,6 +425,21 @@ struct Ring {
     int n;
 };
 
+// Drop from vm the entries the shared hot-vertex cache already knows to be
+// visited; the rest go on to the global bitmap.
+template <int K>
+__device__ __forceinline__ unsigned hot_filter(const Lv& lv, const int (&v)[K], unsigned vm) {
+    if (!lv.hot) return vm;
+    const unsigned* hc = hot_cache();
+    unsigned hw[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) hw[j] = ((vm >> j & 1) && (unsigned)v[j] < lv.hot) ? hc[v[j] >> 5] : 0u;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+        if ((hw[j] >> (v[j] & 31)) & 1u) vm &= ~(1u << j);
+    return vm;
+}
+
 // Pieces of a list [st, st + dg) cut at multiples of the piece size counted
 // from its 16-byte aligned floor a0 = st & ~3: every piece's staged span is
 // at most piece_edges entries and starts aligned.
@@ -674,21 +689,6 @@ __device__ __forceinline__ void ring_drain(const Params& p, const Lv& lv, Tally&
         r.n -= take;
         claim4<PAR>(p, lv, t, v, vm, par);
     }
-}
-
-// Drop from vm the entries the shared hot-vertex cache already knows to be
-// visited; the rest go on to the global bitmap.
-template <int K>
-__device__ __forceinline__ unsigned hot_filter(const Lv& lv, const int (&v)[K], unsigned vm) {
-    if (!lv.hot) return vm;
-    const unsigned* hc = hot_cache();
-    unsigned hw[K];
-#pragma unroll
-    for (int j = 0; j < K; ++j) hw[j] = ((vm >> j & 1) && (unsigned)v[j] < lv.hot) ? hc[v[j] >> 5] : 0u;
-#pragma unroll
-    for (int j = 0; j < K; ++j)
-        if ((hw[j] >> (v[j] & 31)) & 1u) vm &= ~(1u << j);
-    return vm;
 }
 
 // Probe levels: test up to four neighbours per lane against the visited
@@ -1070,9 +1070,13 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         lv.cslot = (L + 1) % 3;
         lv.qn = cur ^ 1;
         {
-            // a block keeps at most about twice its fair share of a frontier
-            // of this level's size; the rest is shared through the global queue
-            const int share = (pushed + gsize - 1) / gsize;
+            // a block keeps at most about twice its fair share of what this
+            // level may discover - at least the frontier's size, and up to an
+            // eighth of its edges (levels around hubs discover far more
+            // vertices than they expand); the rest is shared through the
+            // global queue
+            const int out = max(pushed, sh.in[4] >> 3);
+            const int share = (int)(((long long)out + gsize - 1) / gsize);
             lv.cap = min(p.local_cap, max(32, 2 * share));
         }
         // probe-then-claim where the level scans many edges (most of them hit
@@ -1081,13 +1085,15 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         // grid; 2 = decide per level
         lv.probe = p.probe_first == 2 ? (sh.in[4] >= 128 * nwarps ? 1 : 0) : p.probe_first;
         // direction (Beamer, Asanovic and Patterson, SC 2012): go bottom-up when
-        // the frontier's edges exceed 1/14 of the edges of unvisited vertices,
-        // back to top-down once the frontier falls below n/24 and shrinks.
+        // the frontier grows and its edges exceed 1/14 of the edges of
+        // unvisited vertices, back to top-down once the frontier falls below
+        // n/24 and shrinks (a small frontier late in the search stays
+        // top-down: a bottom-up level would read every vertex's level).
         // Every block sees the same counters, so all decide alike.
         explored += sh.in[4];
         if (p.direction) {
             const long long unexplored = (long long)p.e - explored;
-            if (!bottom_up && 14LL * sh.in[4] > unexplored) bottom_up = true;
+            if (!bottom_up && pushed > prev_pushed && 14LL * sh.in[4] > unexplored) bottom_up = true;
             else if (bottom_up && 24LL * pushed < (long long)p.n && pushed < prev_pushed) bottom_up = false;
         }
         prev_pushed = pushed;
