@@ -96,7 +96,7 @@ int validate_opts(const dfq_opts& o) {
     if (o.direction != 0 && o.direction != 1) return fail(DFQ_EINVAL, "direction must be 0 or 1");
     if (o.vertex_order < 0 || o.vertex_order > 2) return fail(DFQ_EINVAL, "vertex_order must be 0, 1 or 2");
     const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true);
-    const int need = L.bytes + (o.hot_cache >= 0 ? 4 * dfqk::kHotWordsMax : 0);
+    const int need = L.bytes + (o.hot_cache == 1 ? 4 * dfqk::kHotWordsMax : 0);
     if (need > 227 * 1024)
         return fail(DFQ_EINVAL, "options need %d bytes of shared memory per block (max 232448)", need);
     return DFQ_OK;
@@ -367,9 +367,8 @@ int check_symmetric(dfq_graph* g) {
 }
 
 // Shared-memory words of the hot-vertex cache for a graph of bitmap_words.
-int hot_words_for(const dfq_opts& o, int n, bool hub_first) {
-    const bool on = o.hot_cache == 1 || (o.hot_cache == 0 && hub_first);
-    return on ? dfqk::hot_words_of(dfqk::kHotWordsMax, n) : 0;
+int hot_words_for(const dfq_opts& o, int n) {
+    return o.hot_cache == 1 ? dfqk::hot_words_of(dfqk::kHotWordsMax, n) : 0;
 }
 
 // Queue control-block reset + the cooperative kernel on g->stream.
@@ -379,7 +378,7 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     KernelFn k = pick_kernel(o.block_threads, par);
     if (!k) return fail(DFQ_EINVAL, "no kernel for block_threads=%d", o.block_threads);
     const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
-    const int hot_words = hot_words_for(o, g->n, g->relabeled);
+    const int hot_words = hot_words_for(o, g->n);
     const int smem = lay.bytes + 4 * hot_words;
     CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per_sm = 0;

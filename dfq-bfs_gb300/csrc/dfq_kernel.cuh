@@ -406,7 +406,9 @@ struct Lv {
 // global bitmap".
 __device__ __forceinline__ unsigned* hot_cache() { return reinterpret_cast<unsigned*>(dfq_smem + sh.hot_off); }
 
-// Record in the shared cache that v is visited (v < lv.hot).
+// Record in the shared cache that v is visited (v < lv.hot).  Done for the
+// block's own claims only: learning from every probe that finds a visited
+// vertex costs more shared-memory atomics than it saves.
 __device__ __forceinline__ void hot_learn(const Lv& lv, int v) {
     if ((unsigned)v < lv.hot) atomicOr(&hot_cache()[v >> 5], 1u << (v & 31));
 }
@@ -707,11 +709,8 @@ __device__ __forceinline__ void probe4(const Params& p, const Lv& lv, Tally& t, 
     for (int j = 0; j < 4; ++j) w[j] = (vmask >> j & 1) ? p.bitmap[v[j] >> 5] : 0xffffffffu;
     unsigned cm = 0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        if (!(vmask >> j & 1)) continue;
-        if (!((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
-        else hot_learn(lv, v[j]);
-    }
+    for (int j = 0; j < 4; ++j)
+        if ((vmask >> j & 1) && !((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
     const int c = __popc(cm);
     int incl = c;
 #pragma unroll
@@ -752,11 +751,8 @@ __device__ __forceinline__ void probe8(const Params& p, const Lv& lv, Tally& t, 
     for (int j = 0; j < 8; ++j) w[j] = (vm >> j & 1) ? p.bitmap[v[j] >> 5] : 0xffffffffu;
     unsigned cm = 0;
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        if (!(vm >> j & 1)) continue;
-        if (!((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
-        else hot_learn(lv, v[j]);
-    }
+    for (int j = 0; j < 8; ++j)
+        if ((vm >> j & 1) && !((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
     if (!__any_sync(kFull, cm)) return;
     const int c_lo = __popc(cm & 15u), c_hi = __popc(cm >> 4);
     int incl = c_lo | (c_hi << 16);
