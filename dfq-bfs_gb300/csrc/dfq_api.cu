@@ -676,6 +676,7 @@ int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels) {
         o.probe = c.trace_probe[i];
         o.last_done_ns = (int64_t)c.trace_done_last[i];
         o.first_done_ns = c.trace_done_first[i] ? (int64_t)~c.trace_done_first[i] : 0;
+        for (int k = 0; k < 4; ++k) o.phase_ns[k] = (int32_t)c.trace_phase[i][k];
     }
     return n;
 }

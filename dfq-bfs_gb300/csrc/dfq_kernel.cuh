@@ -91,6 +91,9 @@ struct Control {
     int trace_probe[kTraceLevels];      // 1 if level L probed the bitmap before claiming
     unsigned long long trace_done_last[kTraceLevels];   // latest block finish
     unsigned long long trace_done_first[kTraceLevels];  // ~(earliest block finish), 0 = none
+    // with profiling: the latest time (ns after its block's level start) a
+    // warp finished the own queue, the pieces, the overflow chunks, the claims
+    unsigned trace_phase[kTraceLevels][4];
 };
 
 struct Params {
@@ -385,6 +388,7 @@ struct BlockShared {
     unsigned long long large;       // entries this block sent to the large queue (whole BFS)
     unsigned long long red[2];
     int hot_off;                    // byte offset of the hot-vertex cache in dynamic shared memory
+    unsigned long long level_t0[32];  // profiling: when each warp started the level
 };
 static __shared__ BlockShared sh;
 extern __shared__ __align__(128) unsigned char dfq_smem[];
@@ -1094,6 +1098,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         }
         prev_pushed = pushed;
         lv.bottom_up = bottom_up ? 1 : 0;
+        if (p.profile && lane == 0) sh.level_t0[warp] = globaltimer();
         // probe levels consult the shared hot-vertex cache, refreshed here from
         // the global bitmap (everything visited before this level) and added
         // to during the level as this block meets visited vertices
@@ -1121,17 +1126,20 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             // the frontier is read from the levels; this level's queues are not expanded
             bottom_up_level<PAR>(p, lv, t, gwarp, nwarps);
         } else {
-            // (1) this block's own queue from the previous level, 32 entries per grab
+            // (1) this block's own queue from the previous level; a short queue
+            //     is shared by all the block's warps (a few entries per grab),
+            //     since its lists may be long and a warp expands them in turn
             {
                 const int nloc = sh.cnt_cur;
+                const int grab = min(32, max(1, (nloc + NW - 1) / NW));
                 const int* qc = reinterpret_cast<const int*>(dfq_smem) + cur * 3 * p.local_cap;
                 while (true) {
                     int j = 0;
-                    if (lane == 0) j = atomicAdd(&sh.local_grab, 32);
+                    if (lane == 0) j = atomicAdd(&sh.local_grab, grab);
                     j = __shfl_sync(kFull, j, 0);
                     if (j >= nloc) break;
                     const int i = j + lane;
-                    const bool has = i < nloc;
+                    const bool has = lane < grab && i < nloc;
                     warp_process<PAR>(p, lv, t, ring, wl, has, has ? qc[i] : 0, has ? qc[p.local_cap + i] : 0,
                                       (PAR && has) ? qc[2 * p.local_cap + i] : 0);
                 }
@@ -1142,6 +1150,8 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             //     there are no more pieces than warps each piece goes to one warp;
             //     otherwise the first 3/4 go round-robin and the rest are pulled
             //     from a counter
+                if (p.profile && lane == 0 && L < kTraceLevels)
+                    atomicMax(&ctl->trace_phase[L][0], (unsigned)(globaltimer() - sh.level_t0[warp]));
             if (total_pieces > 0 && !warp_failed) {
                 const int2* pin = p.piece[in];
                 const int* pvin = p.piece_v[in];
@@ -1239,13 +1249,18 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                 }
             }
 
-            // (3) global overflow queue in 32-entry chunks, same schedule as the
+                if (p.profile && lane == 0 && L < kTraceLevels)
+                    atomicMax(&ctl->trace_phase[L][1], (unsigned)(globaltimer() - sh.level_t0[warp]));
+            // (3) global overflow queue in chunks, same schedule as the
             //     pieces; the next chunk index is fetched before the current one
             //     is expanded
             if (n_ovf > 0) {
                 const int2* ovf_in = p.ovf[in];
                 const int* ovfv_in = p.ovfv[in];
-                const int n_chunks = (n_ovf + 31) >> 5;
+                // chunks of up to 32 entries; a short queue is cut finer so its
+                // (possibly long) lists spread over the group's warps
+                const int csz = min(32, max(1, (n_ovf + nwarps - 1) / nwarps));
+                const int n_chunks = (n_ovf + csz - 1) / csz;
                 const int c_static = n_chunks <= nwarps ? n_chunks : n_chunks - (n_chunks >> 2);
                 int s_next = gwarp;
                 auto next_chunk = [&]() -> int {  // lane 0 only
@@ -1258,10 +1273,10 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                 while (true) {
                     const int ci = __shfl_sync(kFull, nxt, 0);
                     if (ci >= n_chunks) break;
-                    const int c0 = ci << 5;
+                    const int c0 = ci * csz;
                     if (lane == 0) nxt = next_chunk();
                     const int i = c0 + lane;
-                    const bool has = i < n_ovf;
+                    const bool has = lane < csz && i < n_ovf;
                     int2 x = make_int2(0, 0);
                     int u = 0;
                     if (has) {
@@ -1273,7 +1288,13 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             }
         }
         // claim whatever candidates this warp still holds
+        if (!lv.bottom_up) {
+            if (p.profile && lane == 0 && L < kTraceLevels)
+                atomicMax(&ctl->trace_phase[L][2], (unsigned)(globaltimer() - sh.level_t0[warp]));
+        }
         ring_drain<PAR>(p, lv, t, ring, true);
+        if (p.profile && lane == 0 && L < kTraceLevels)
+            atomicMax(&ctl->trace_phase[L][3], (unsigned)(globaltimer() - sh.level_t0[warp]));
 
         // end of level: publish how much this block pushed, keep its queue
         __syncthreads();

@@ -96,7 +96,7 @@ class ServerResult(C.Structure):
 class LevelInfo(C.Structure):
     _fields_ = [("start_ns", C.c_int64), ("first_done_ns", C.c_int64), ("last_done_ns", C.c_int64),
                 ("frontier", C.c_int32), ("edges", C.c_int32), ("overflow", C.c_int32),
-                ("pieces", C.c_int32), ("probe", C.c_int32), ("pad", C.c_int32)]
+                ("pieces", C.c_int32), ("probe", C.c_int32), ("pad", C.c_int32), ("phase_ns", C.c_int32 * 4)]
 
 
 class Stats(C.Structure):
@@ -417,6 +417,7 @@ class Graph:
             row = {"frontier": r.frontier, "edges": r.edges, "overflow": r.overflow, "pieces": r.pieces,
                    "probe": r.probe}
             if r.last_done_ns:
+                row["us_phases"] = [round(x / 1e3, 2) for x in r.phase_ns]
                 row["us_work"] = (r.last_done_ns - r.start_ns) / 1e3
                 row["us_spread"] = (r.last_done_ns - r.first_done_ns) / 1e3
                 if i + 1 < k:

@@ -248,6 +248,9 @@ typedef struct dfq_level_info {
     int32_t pieces;         /* large-list pieces */
     int32_t probe;          /* 1: probe-then-claim level, 0: claim at once, 2: bottom-up */
     int32_t pad;
+    /* with profile: over all warps, the latest time (ns after the warp began the level) a warp
+     * finished its block's own queue, the large-list pieces, the overflow queue, and its claims */
+    int32_t phase_ns[4];
 } dfq_level_info;
 int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels);
 
