@@ -58,6 +58,8 @@ struct dfq_graph {
     int32_t* order = nullptr;
     int32_t* levels_int = nullptr;   // levels / parents by new id
     int32_t* parents_int = nullptr;
+    unsigned* hub_claim = nullptr;   // claim words of the first hub_n (new) ids
+    int hub_n = 0;
 };
 
 namespace {
@@ -232,6 +234,7 @@ void release(dfq_graph* g) {
     cudaFree(g->order);
     cudaFree(g->levels_int);
     cudaFree(g->parents_int);
+    cudaFree(g->hub_claim);
     if (g->ctl_host) cudaFreeHost(g->ctl_host);
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
@@ -345,6 +348,9 @@ int maybe_relabel(dfq_graph* g) {
     g->cols = cols_d;
     g->rank_host = std::move(rank);
     g->relabeled = true;
+    // hubs (now the smallest ids) get claim words of their own
+    g->hub_n = std::min<int32_t>(n, 32768);
+    if ((rc = dev_alloc(&g->hub_claim, (size_t)g->hub_n * dfqk::kHubStride))) return rc;
     return DFQ_OK;
 }
 
@@ -432,6 +438,8 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
         p.parents_out = parents;
         p.rank = g->rank;
         p.order = g->order;
+        p.hub_claim = g->hub_claim;
+        p.hub_n = g->hub_n;
     }
 
     CUDA_TRY(cudaMemsetAsync(g->ctl, 0, sizeof(dfqk::Control), g->stream));

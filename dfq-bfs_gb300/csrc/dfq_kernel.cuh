@@ -134,7 +134,16 @@ struct Params {
     const int* order;
     int* levels_out;
     int* parents_out;
+    // hub claim words: vertices below hub_n are claimed through their own
+    // word, kHubStride apart, instead of a bit of the shared bitmap (null: off)
+    unsigned* hub_claim;
+    int hub_n;
 };
+
+// Hub claim words sit a 32-byte sector apart: with hub-first ids ~1000 hubs
+// share one 128-byte bitmap line, and claim atomics on one line serialise in
+// L2 (a level around hubs makes hundreds of thousands of them).
+constexpr int kHubStride = 8;
 
 // Pieces one level can produce with pieces of at least min_piece (>= 64)
 // edges and large lists of at least min_large edges: a list of degree d cut
@@ -400,6 +409,7 @@ struct Lv {
     int cslot;  // counter slot of the output frontier (L + 1) % 3
     int qn;     // local queue buffer being filled
     int cap;    // entries this block may keep locally at this level
+    int ecap;   // edges (degree sum) this block may keep locally at this level
     int probe;  // probe the bitmap before claiming
     unsigned hot;  // vertices below this id have visited bits in the shared cache (0: none)
     int bottom_up; // this level: every unvisited vertex looks for a parent in the frontier
@@ -493,7 +503,7 @@ __device__ __forceinline__ void push_claims(const Params& p, const Lv& lv, unsig
             unsigned long long old = *(volatile unsigned long long*)&sh.local_pack;
             while (true) {
                 const unsigned n_ent = (unsigned)(old >> 32), n_deg = (unsigned)old;
-                if (n_ent + (unsigned)tot > (unsigned)lv.cap || n_deg + (unsigned)tsum > (unsigned)p.local_budget)
+                if (n_ent + (unsigned)tot > (unsigned)lv.cap || n_deg + (unsigned)tsum > (unsigned)lv.ecap)
                     break;
                 const unsigned long long want =
                     ((unsigned long long)(n_ent + tot) << 32) | (unsigned long long)(n_deg + (unsigned)tsum);
@@ -569,7 +579,7 @@ __device__ __forceinline__ void push_claims(const Params& p, const Lv& lv, unsig
     unsigned poff = pbase + (unsigned)((incl & 0xffffff) - npl);
     int2* pc = lv.out ? p.piece[1] : p.piece[0];
     int* pv = lv.out ? p.piece_v[1] : p.piece_v[0];
-    constexpr int kOwn = 4;
+    constexpr int kOwn = 32;  // per lane up to this many pieces; giants cooperatively
     unsigned big = 0;
     unsigned boff[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
@@ -627,8 +637,15 @@ __device__ __forceinline__ void claim4(const Params& p, const Lv& lv, Tally& t, 
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         if (!(vm >> j & 1)) continue;
+        // a hub is claimed on its own word (its winner then sets its bitmap
+        // bit for the probes: one atomic per hub there); others on the bitmap
+        const bool hub = v[j] < p.hub_n;
         const unsigned bit = 1u << (v[j] & 31);
-        if (!(atomicOr(&p.bitmap[v[j] >> 5], bit) & bit)) won |= 1u << j;
+        unsigned* word = hub ? p.hub_claim + v[j] * kHubStride : p.bitmap + (v[j] >> 5);
+        if (!(atomicOr(word, bit) & bit)) {
+            won |= 1u << j;
+            if (hub) atomicOr(&p.bitmap[v[j] >> 5], bit);
+        }
         hot_learn(lv, v[j]);  // visited now, whoever won
     }
     int st[4], dg[4];
@@ -942,6 +959,7 @@ __device__ __forceinline__ void bottom_up_level(const Params& p, const Lv& lv, T
             p.levels[v] = lv.next;
             if (PAR) p.parents[v] = par;
             atomicOr(&p.bitmap[v >> 5], 1u << (v & 31));
+            if (v < p.hub_n) p.hub_claim[v * kHubStride] = 1u << (v & 31);
             t.claims += 1;
             sh.claimed = 1;
             st[0] = s0;
@@ -996,6 +1014,8 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         }
         for (long long w = gtid; w < p.bitmap_words; w += nth)
             p.bitmap[w] = (w == (src >> 5)) ? (1u << (src & 31)) : 0u;
+        for (long long h = gtid; h < p.hub_n; h += nth)
+            p.hub_claim[h * kHubStride] = (h == src) ? (1u << (src & 31)) : 0u;
         if (gtid == 0) {
             const int s0 = p.offsets[src], d = p.offsets[src + 1] - s0;
             if (d > 0) {
@@ -1078,6 +1098,11 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             const int out = max(pushed, sh.in[4] >> 3);
             const int share = (int)(((long long)out + gsize - 1) / gsize);
             lv.cap = min(p.local_cap, max(32, 2 * share));
+            // likewise in edges: while the frontier is small, the lists a block
+            // finds (around hubs, long ones) go to the shared queue, where all
+            // warps of the group can take them, instead of its own few warps
+            const long long eshare = ((long long)sh.in[4] + gsize - 1) / gsize;
+            lv.ecap = (int)min((long long)p.local_budget, max(1024LL, 2 * eshare));
         }
         // probe-then-claim where the level scans many edges (most of them hit
         // visited vertices); claim at once, with row bounds fetched alongside,
