@@ -1147,6 +1147,9 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             atomicAdd(&ctl->stats.edges, (unsigned long long)(unsigned)sh.in[4]);
         }
 
+        // frontier lists averaging 16+ edges: short queues are split finely
+        // over the warps; shorter lists are best gathered 32 to a warp
+        const bool fine = sh.in[4] >= 16 * max(pushed, 1);
         if (lv.bottom_up) {
             // the frontier is read from the levels; this level's queues are not expanded
             bottom_up_level<PAR>(p, lv, t, gwarp, nwarps);
@@ -1156,7 +1159,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             //     since its lists may be long and a warp expands them in turn
             {
                 const int nloc = sh.cnt_cur;
-                const int grab = min(32, max(1, (nloc + NW - 1) / NW));
+                const int grab = fine ? min(32, max(1, (nloc + NW - 1) / NW)) : 32;
                 const int* qc = reinterpret_cast<const int*>(dfq_smem) + cur * 3 * p.local_cap;
                 while (true) {
                     int j = 0;
@@ -1284,7 +1287,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                 const int* ovfv_in = p.ovfv[in];
                 // chunks of up to 32 entries; a short queue is cut finer so its
                 // (possibly long) lists spread over the group's warps
-                const int csz = min(32, max(1, (n_ovf + nwarps - 1) / nwarps));
+                const int csz = fine ? min(32, max(1, (n_ovf + nwarps - 1) / nwarps)) : 32;
                 const int n_chunks = (n_ovf + csz - 1) / csz;
                 const int c_static = n_chunks <= nwarps ? n_chunks : n_chunks - (n_chunks >> 2);
                 int s_next = gwarp;
