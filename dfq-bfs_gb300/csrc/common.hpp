@@ -48,6 +48,15 @@ struct EdgeSpan {
 // flags as for dfq_csr_from_edges.  Same result for any host thread count.
 int build_csr(const std::vector<EdgeSpan>& spans, int32_t n, int32_t flags, dfq_csr* out);
 
+// Hub-first renumbering of a host CSR: new id i is input id order[i], sorted
+// by descending in-degree (ties by id), rank[v] the new id of v; each row of
+// out lists its neighbours in new ids with the row's hub (smallest new id)
+// first.  mode as dfq_opts.vertex_order (0 auto: at least 2^16 vertices and
+// a largest in-degree >= 64 x the average; 1 never; 2 always).  Returns 1 if
+// renumbered (out allocated), 0 if not, or a negative status.
+int hub_first_csr(const dfq_csr& in, int mode, dfq_csr* out, std::vector<int32_t>* rank,
+                  std::vector<int32_t>* order);
+
 // Run body(i) for i in [0, t) on t threads (the caller's thread takes i = 0).
 template <class F>
 void run_threads(int t, F&& body) {

@@ -77,6 +77,7 @@ __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, i
     sp.use_tma = bp.use_tma;
     sp.timeout_ns = bp.timeout_ns;
     sp.hot_words = hot_words_of(bp.hot_words, g.n);
+    remap_params(sp, g, ws);  // renumbered graphs are wide: only the grid's workspace has room
 }
 
 // This block's narrow-query workspace.
@@ -92,6 +93,9 @@ __device__ __forceinline__ Workspace block_workspace(const BatchParams& bp) {
         bw.piece_v[i] = (int*)(base + l.piece_v[i]);
     }
     bw.piece_cap = l.piece_cap;
+    bw.levels_int = nullptr;  // one-block workspaces take no renumbered graph
+    bw.parents_int = nullptr;
+    bw.hub_claim = nullptr;
     return bw;
 }
 
@@ -286,19 +290,46 @@ int dfq_pool_create(const dfq_csr* graphs, int32_t ngraphs, const dfq_opts* opts
     P_TRY(dmalloc(&p->cols, sizeof(int32_t) * (size_t)tot_e));
     P_CUDA(cudaMemsetAsync(p->cols, 0, sizeof(int32_t) * (size_t)tot_e, p->stream));
     for (int i = 0; i < ngraphs; ++i) {
-        const dfq_csr& g = graphs[i];
+        // wide graphs with skewed degrees are stored hub-first (as dfq_graph_create does)
+        dfq_csr rg;
+        memset(&rg, 0, sizeof rg);
+        std::vector<int32_t> rank, order;
+        int relabeled = 0;
+        if (p->wide[i]) {
+            relabeled = hub_first_csr(graphs[i], o.vertex_order, &rg, &rank, &order);
+            if (relabeled < 0) { pool_release(p); return relabeled; }
+        }
+        const dfq_csr& g = relabeled ? rg : graphs[i];
         P_CUDA(cudaMemcpyAsync(p->offsets + off_base[i], g.offsets, sizeof(int32_t) * ((size_t)g.n + 1),
                                cudaMemcpyHostToDevice, p->stream));
         if (g.e) P_CUDA(cudaMemcpyAsync(p->cols + col_base[i], g.cols, sizeof(int32_t) * (size_t)g.e,
                                         cudaMemcpyHostToDevice, p->stream));
+        const int32_t* d_rank = nullptr;
+        const int32_t* d_order = nullptr;
+        if (relabeled) {
+            int32_t *a = nullptr, *b = nullptr;
+            int rc = dmalloc(&a, sizeof(int32_t) * (size_t)g.n);
+            if (rc == DFQ_OK) p->remap_arrays.push_back(a);
+            if (rc == DFQ_OK) rc = dmalloc(&b, sizeof(int32_t) * (size_t)g.n);
+            if (rc == DFQ_OK) p->remap_arrays.push_back(b);
+            if (rc) { dfq_csr_free(&rg); pool_release(p); return rc; }
+            cudaMemcpyAsync(a, rank.data(), sizeof(int32_t) * (size_t)g.n, cudaMemcpyHostToDevice, p->stream);
+            cudaMemcpyAsync(b, order.data(), sizeof(int32_t) * (size_t)g.n, cudaMemcpyHostToDevice, p->stream);
+            d_rank = a;
+            d_order = b;
+        }
         PoolGraph pg;
+        pg.rank = d_rank;
+        pg.order = d_order;
         pg.offsets = p->offsets + off_base[i];
         pg.cols = p->cols + col_base[i];
         pg.n = g.n;
         pg.wide = p->wide[i];
         pg.e = g.e;
         p->h_graphs.push_back(pg);
-        P_CUDA(cudaStreamSynchronize(p->stream));  // host CSR may be pageable
+        const cudaError_t serr = cudaStreamSynchronize(p->stream);  // host arrays may be pageable / are freed now
+        dfq_csr_free(&rg);
+        P_CUDA(serr);
     }
     P_TRY(dmalloc(&p->d_graphs, sizeof(PoolGraph) * ngraphs));
     P_CUDA(cudaMemcpyAsync(p->d_graphs, p->h_graphs.data(), sizeof(PoolGraph) * ngraphs, cudaMemcpyHostToDevice,
@@ -378,6 +409,7 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     prm.use_tma = o.use_tma;
     prm.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     prm.hot_words = hot;
+    remap_params(prm, p->h_graphs[graph], w);
     cudaEventRecord(p->ev0, p->stream);
     cudaMemsetAsync(p->d_ctl1, 0, sizeof(Control), p->stream);
     if ((rc = launch_coop(fn, grid, o.block_threads, smem, &prm, p->stream))) return rc;

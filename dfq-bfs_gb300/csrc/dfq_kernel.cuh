@@ -138,12 +138,14 @@ struct Params {
     // word, kHubStride apart, instead of a bit of the shared bitmap (null: off)
     unsigned* hub_claim;
     int hub_n;
+    int map_src;  // 1: src is an input id, renumbered here through rank
 };
 
 // Hub claim words sit a 32-byte sector apart: with hub-first ids ~1000 hubs
 // share one 128-byte bitmap line, and claim atomics on one line serialise in
 // L2 (a level around hubs makes hundreds of thousands of them).
 constexpr int kHubStride = 8;
+constexpr int kHubIds = 32768;  // hub claim words per renumbered graph
 
 // Pieces one level can produce with pieces of at least min_piece (>= 64)
 // edges and large lists of at least min_large edges: a list of degree d cut
@@ -1004,7 +1006,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
     Control* ctl = p.ctl;
 
     // ---- init: levels, parents, bitmap (source pre-set so no ordering is needed)
-    const int src = p.src;
+    const int src = p.map_src ? __ldg(p.rank + p.src) : p.src;
     {
         const long long gtid = (long long)grank * B + tid;
         const long long nth = (long long)gsize * B;

@@ -18,6 +18,8 @@ struct PoolGraph {
     int n;
     int wide;
     long long e;
+    const int* rank;   // hub-first renumbered graph: new id of each input id (else null)
+    const int* order;  //   and input id of each new id
 };
 
 // One query as the device sees it; start/end written by the kernel.
@@ -38,26 +40,51 @@ struct Workspace {
     int2* piece[2];
     int* piece_v[2];
     int piece_cap;
+    int* levels_int;      // renumbered graphs: levels / parents by new id (else null)
+    int* parents_int;
+    unsigned* hub_claim;  //   and the hubs' claim words
 };
 
 // Byte layout of one workspace for graphs up to n vertices and e edges.
 struct WsLayout {
-    size_t bitmap, ovf[2], ovfv[2], piece[2], piece_v[2], total;
+    size_t bitmap, ovf[2], ovfv[2], piece[2], piece_v[2], levels_int, parents_int, hub_claim, total;
     int piece_cap;
+    bool remap;
 };
 
 inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
-inline WsLayout ws_layout(long long n, long long e, int min_large, int min_piece, bool par) {
+// remap: room for a renumbered graph's levels / parents by new id and hub claim words
+inline WsLayout ws_layout(long long n, long long e, int min_large, int min_piece, bool par, bool remap = false) {
     WsLayout w;
     size_t o = 0;
+    w.remap = remap;
     w.bitmap = o;  o = al256(o + 4 * (size_t)(((n + 31) / 32 + 31) & ~31LL));
     w.piece_cap = piece_capacity(n, e, min_large, min_piece);
     for (int i = 0; i < 2; ++i) { w.ovf[i] = o;   o = al256(o + 8 * (size_t)std::max<long long>(n, 1)); }
     for (int i = 0; i < 2; ++i) { w.ovfv[i] = o;  o = al256(o + (par ? 4 * (size_t)std::max<long long>(n, 1) : 256)); }
     for (int i = 0; i < 2; ++i) { w.piece[i] = o;   o = al256(o + 8 * (size_t)w.piece_cap); }
     for (int i = 0; i < 2; ++i) { w.piece_v[i] = o; o = al256(o + (par ? 4 * (size_t)w.piece_cap : 256)); }
+    w.levels_int = o; o = al256(o + (remap ? 4 * (size_t)std::max<long long>(n, 1) : 256));
+    w.parents_int = o; o = al256(o + (remap && par ? 4 * (size_t)std::max<long long>(n, 1) : 256));
+    w.hub_claim = o;  o = al256(o + (remap ? 4 * (size_t)kHubStride * kHubIds : 256));
     w.total = o;
     return w;
+}
+
+// A query on a renumbered graph (g.rank != null) in a workspace with room for
+// it: the kernel runs on new ids into the workspace's arrays and writes the
+// caller's levels / parents in input ids at the end.
+__host__ __device__ inline void remap_params(Params& sp, const PoolGraph& g, const Workspace& ws) {
+    if (!g.rank || !ws.levels_int) return;
+    sp.levels_out = sp.levels;
+    sp.parents_out = sp.parents;
+    sp.levels = ws.levels_int;
+    sp.parents = sp.parents ? ws.parents_int : nullptr;
+    sp.rank = g.rank;
+    sp.order = g.order;
+    sp.map_src = 1;
+    sp.hub_claim = ws.hub_claim;
+    sp.hub_n = g.n < kHubIds ? g.n : kHubIds;
 }
 
 }  // namespace dfqk
@@ -109,6 +136,7 @@ struct dfq_pool {
     // single-query launches
     Control* d_ctl1 = nullptr;
     Control* h_ctl1 = nullptr;
+    std::vector<int32_t*> remap_arrays;  // rank / order of the renumbered graphs
 };
 
 namespace dfqpool {
@@ -147,6 +175,7 @@ inline void pool_release(dfq_pool* p) {
     cudaFree(p->d_misc);
     cudaFree(p->d_t0);
     cudaFree(p->d_ctl1);
+    for (int32_t* a : p->remap_arrays) cudaFree(a);
     if (p->h_queries) cudaFreeHost(p->h_queries);
     if (p->h_lists) cudaFreeHost(p->h_lists);
     if (p->h_ctls) cudaFreeHost(p->h_ctls);
@@ -168,6 +197,9 @@ inline Workspace ws_from(unsigned char* base, const WsLayout& l) {
         w.piece_v[i] = (int*)(base + l.piece_v[i]);
     }
     w.piece_cap = l.piece_cap;
+    w.levels_int = l.remap ? (int*)(base + l.levels_int) : nullptr;
+    w.parents_int = l.remap ? (int*)(base + l.parents_int) : nullptr;
+    w.hub_claim = l.remap ? (unsigned*)(base + l.hub_claim) : nullptr;
     return w;
 }
 
@@ -179,7 +211,9 @@ inline int ensure_wide(dfq_pool* p, bool par) {
     p->wide_mem = nullptr;
     long long nmax = 1, emax = 0;
     for (int i = 0; i < p->ngraphs; ++i) { nmax = std::max<long long>(nmax, p->n[i]); emax = std::max<long long>(emax, p->e[i]); }
-    p->wide_lay = ws_layout(nmax, emax, kMinLarge, kMinPiece, par);
+    bool remap = false;
+    for (const PoolGraph& g : p->h_graphs) remap = remap || g.rank != nullptr;
+    p->wide_lay = ws_layout(nmax, emax, kMinLarge, kMinPiece, par, remap);
     p->wide_par = par;
     return dmalloc(&p->wide_mem, p->wide_lay.total);
 }

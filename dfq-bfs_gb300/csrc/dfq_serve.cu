@@ -141,6 +141,7 @@ __device__ __forceinline__ void serve_params(Params& sp, const ServeParams& s, c
     sp.use_tma = s.use_tma;
     sp.timeout_ns = s.timeout_ns;
     sp.hot_words = hot_words_of(s.hot_words, g.n);
+    remap_params(sp, g, ws);  // renumbered graphs are wide: only the gang's workspace has room
 }
 
 // Copy one ring slot (seq checked: the host writes the fields before the count).
@@ -220,6 +221,9 @@ __device__ __forceinline__ Workspace block_workspace(const ServeParams& s) {
         bw.piece_v[i] = (int*)(base + s.block_lay.piece_v[i]);
     }
     bw.piece_cap = s.block_lay.piece_cap;
+    bw.levels_int = nullptr;  // one-block workspaces take no renumbered graph
+    bw.parents_int = nullptr;
+    bw.hub_claim = nullptr;
     return bw;
 }
 

@@ -227,6 +227,50 @@ int build_csr(const std::vector<EdgeSpan>& spans, int32_t n, int32_t flags, dfq_
     return DFQ_OK;
 }
 
+int hub_first_csr(const dfq_csr& in, int mode, dfq_csr* out, std::vector<int32_t>* rank_out,
+                  std::vector<int32_t>* order_out) {
+    const int32_t n = in.n;
+    const int64_t e = in.e;
+    if (mode == 1 || n < 1 || e == 0) return 0;
+    std::vector<int32_t> indeg((size_t)n, 0);
+    for (int64_t k = 0; k < e; ++k) indeg[in.cols[k]]++;
+    const int32_t mx = *std::max_element(indeg.begin(), indeg.end());
+    if (mode == 0 && (n < (1 << 16) || (double)mx < 64.0 * ((double)e / (double)n))) return 0;
+    std::vector<int32_t>& order = *order_out;
+    std::vector<int32_t>& rank = *rank_out;
+    order.resize(n);
+    rank.resize(n);
+    if ((int64_t)mx <= 4 * (int64_t)n + 1024) {  // stable counting sort by descending in-degree
+        std::vector<int64_t> at((size_t)mx + 2, 0);
+        for (int32_t v = 0; v < n; ++v) at[(size_t)(mx - indeg[v]) + 1]++;
+        for (size_t k = 1; k < at.size(); ++k) at[k] += at[k - 1];
+        for (int32_t v = 0; v < n; ++v) order[at[(size_t)(mx - indeg[v])]++] = v;
+    } else {
+        for (int32_t v = 0; v < n; ++v) order[v] = v;
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return indeg[a] > indeg[b]; });
+    }
+    for (int32_t i = 0; i < n; ++i) rank[order[i]] = i;
+    int rc = alloc_csr(n, e, out);
+    if (rc) return rc;
+    out->source = in.source;
+    out->offsets[0] = 0;
+    for (int32_t i = 0; i < n; ++i) out->offsets[i + 1] = out->offsets[i] + (in.offsets[order[i] + 1] - in.offsets[order[i]]);
+    parallel_for(n, [&](int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; ++i) {
+            const int32_t o = order[i];
+            int32_t* row = out->cols + out->offsets[i];
+            const int32_t d = in.offsets[o + 1] - in.offsets[o];
+            int32_t best = 0;
+            for (int32_t k = 0; k < d; ++k) {
+                row[k] = rank[in.cols[in.offsets[o] + k]];
+                if (row[k] < row[best]) best = k;
+            }
+            if (best > 0) std::swap(row[0], row[best]);
+        }
+    }, 1 << 12);
+    return 1;
+}
+
 }  // namespace dfq
 
 using namespace dfq;

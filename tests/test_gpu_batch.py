@@ -137,3 +137,35 @@ def test_batch_rejects_bad_queries(torch):
             pool.batch([(len(graphs), 0, lv)])
         with pytest.raises(d.DfqError):
             pool.batch([(0, graphs[0].n, lv)])
+
+
+def test_renumbered_wide_graphs(torch):
+    """Wide graphs with skewed degrees are stored hub-first in the pool; batch,
+    single launch and server still answer in input ids (levels, trees, E_R)."""
+    graphs = [d.gen_rmat(17, 16, seed=41), d.gen_grid(40, 0.02, seed=41)[0], d.gen_rmat(10, 8, seed=42)]
+    o = d.default_opts()
+    o.wide_min_edges = 1 << 20
+    with d.Pool(graphs, o) as pool:
+        assert pool.info(0)[2] and not pool.info(1)[2]
+        for parents in (False, True):
+            qs, meta = make_queries(torch, graphs, 3, seed=43, parents=parents)
+            res, _ = pool.batch(qs, d.BATCH_GRAPH)
+            check_results(qs, meta, res, parents=parents)
+        g = graphs[0]
+        for s in g.pick_sources(2, seed=44):
+            lv = torch.empty(g.n, dtype=torch.int32, device="cuda")
+            pa = torch.empty(g.n, dtype=torch.int32, device="cuda")
+            pool.bfs(0, int(s), lv, pa)
+            want = oracle.bfs(g.offsets, g.cols, int(s))
+            assert np.array_equal(lv.cpu().numpy(), want)
+            assert oracle.validate_tree(g.offsets, g.cols, int(s), lv.cpu().numpy(), pa.cpu().numpy()) == 0
+        with d.Server(pool, with_parents=True) as srv:
+            ids = {srv.submit(0, int(s)): int(s) for s in g.pick_sources(3, seed=45)}
+            done = srv.drain(60.0)
+            assert {r.id for r in done} == set(ids) and all(r.status == 0 for r in done)
+            for rid, s in ids.items():
+                lv, pa = srv.levels(rid, g.n, parents=True)
+                want = oracle.bfs(g.offsets, g.cols, s)
+                assert np.array_equal(lv, want)
+                assert oracle.validate_tree(g.offsets, g.cols, s, lv, pa) == 0
+                srv.release(rid)
