@@ -400,6 +400,7 @@ struct BlockShared {
     unsigned long long red[2];
     int hot_off;                    // byte offset of the hot-vertex cache in dynamic shared memory
     unsigned long long level_t0[32];  // profiling: when each warp started the level
+    unsigned phase_max[4];            // profiling: this block's latest warp phase ends
 };
 static __shared__ BlockShared sh;
 extern __shared__ __align__(128) unsigned char dfq_smem[];
@@ -1046,6 +1047,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
     if (tid == 0) {
         s_block_err = 0;
         sh.hot_off = lay.hot_off;
+        for (int k = 0; k < 4; ++k) sh.phase_max[k] = 0;
         sh.local_pack = 0ull;
         sh.cnt_cur = sh.local_grab = sh.ovf_pushed = sh.large_pushed = sh.large_pieces = sh.claimed = 0;
         sh.ovf_edges = sh.large_edges = 0;
@@ -1181,7 +1183,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             //     otherwise the first 3/4 go round-robin and the rest are pulled
             //     from a counter
                 if (p.profile && lane == 0 && L < kTraceLevels)
-                    atomicMax(&ctl->trace_phase[L][0], (unsigned)(globaltimer() - sh.level_t0[warp]));
+                    atomicMax(&sh.phase_max[0], (unsigned)(globaltimer() - sh.level_t0[warp]));
             if (total_pieces > 0 && !warp_failed) {
                 const int2* pin = p.piece[in];
                 const int* pvin = p.piece_v[in];
@@ -1280,7 +1282,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             }
 
                 if (p.profile && lane == 0 && L < kTraceLevels)
-                    atomicMax(&ctl->trace_phase[L][1], (unsigned)(globaltimer() - sh.level_t0[warp]));
+                    atomicMax(&sh.phase_max[1], (unsigned)(globaltimer() - sh.level_t0[warp]));
             // (3) global overflow queue in chunks, same schedule as the
             //     pieces; the next chunk index is fetched before the current one
             //     is expanded
@@ -1320,11 +1322,11 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         // claim whatever candidates this warp still holds
         if (!lv.bottom_up) {
             if (p.profile && lane == 0 && L < kTraceLevels)
-                atomicMax(&ctl->trace_phase[L][2], (unsigned)(globaltimer() - sh.level_t0[warp]));
+                atomicMax(&sh.phase_max[2], (unsigned)(globaltimer() - sh.level_t0[warp]));
         }
         ring_drain<PAR>(p, lv, t, ring, true);
         if (p.profile && lane == 0 && L < kTraceLevels)
-            atomicMax(&ctl->trace_phase[L][3], (unsigned)(globaltimer() - sh.level_t0[warp]));
+            atomicMax(&sh.phase_max[3], (unsigned)(globaltimer() - sh.level_t0[warp]));
 
         // end of level: publish how much this block pushed, keep its queue
         __syncthreads();
@@ -1361,6 +1363,10 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             // recorded after the barrier: its release would otherwise wait for them
             atomicMax(&ctl->trace_done_last[L], done_ns);
             atomicMax(&ctl->trace_done_first[L], ~done_ns);
+            for (int k = 0; k < 4; ++k) {
+                atomicMax(&ctl->trace_phase[L][k], sh.phase_max[k]);
+                sh.phase_max[k] = 0;
+            }
         }
     }
 
