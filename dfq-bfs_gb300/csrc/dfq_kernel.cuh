@@ -1184,7 +1184,24 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             //     from a counter
                 if (p.profile && lane == 0 && L < kTraceLevels)
                     atomicMax(&sh.phase_max[0], (unsigned)(globaltimer() - sh.level_t0[warp]));
-            if (total_pieces > 0 && !warp_failed) {
+            // far fewer pieces than warps (a level around a few long lists):
+            // each piece is cut into up to 8 ranges, expanded straight from
+            // global memory by separate warps
+            const int split = total_pieces * 8 <= nwarps ? 8 : total_pieces * 4 <= nwarps ? 4
+                                                             : total_pieces * 2 <= nwarps ? 2 : 1;
+            if (total_pieces > 0 && split > 1) {
+                const int2* pin = p.piece[in];
+                const int* pvin = p.piece_v[in];
+                for (int g = gwarp; g < total_pieces * split; g += nwarps) {
+                    const int k = g / split;
+                    const int2 d = __ldcg(pin + k);
+                    const int par0 = PAR ? __ldcg(pvin + k) : 0;
+                    const int step = (d.y - d.x + split - 1) / split;
+                    const int lo = d.x + (g - k * split) * step;
+                    const int hi = min(d.y, lo + step);
+                    if (hi > lo) warp_expand<PAR>(p, lv, t, ring, lo, hi - lo, par0);
+                }
+            } else if (total_pieces > 0 && !warp_failed) {
                 const int2* pin = p.piece[in];
                 const int* pvin = p.piece_v[in];
                 const int p_static = total_pieces <= nwarps ? total_pieces : total_pieces - total_pieces / 4;
