@@ -93,12 +93,12 @@ int validate_opts(const dfq_opts& o) {
     if (o.local_edge_budget < 0) return fail(DFQ_EINVAL, "local_edge_budget must be >= 0");
     if (o.timeout_ms < 1) return fail(DFQ_EINVAL, "timeout_ms must be >= 1");
     if (o.probe_first < 0 || o.probe_first > 2) return fail(DFQ_EINVAL, "probe_first must be 0, 1 or 2");
-    if (o.hot_cache < -1 || o.hot_cache > 1) return fail(DFQ_EINVAL, "hot_cache must be -1, 0 or 1");
+    if (o.hot_cache < -1 || o.hot_cache > 32) return fail(DFQ_EINVAL, "hot_cache must be -1, 0 or 1..32 (KB)");
     if (o.profile != 0 && o.profile != 1) return fail(DFQ_EINVAL, "profile must be 0 or 1");
     if (o.direction != 0 && o.direction != 1) return fail(DFQ_EINVAL, "direction must be 0 or 1");
     if (o.vertex_order < 0 || o.vertex_order > 2) return fail(DFQ_EINVAL, "vertex_order must be 0, 1 or 2");
     const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true);
-    const int need = L.bytes + (o.hot_cache == 1 ? 4 * dfqk::kHotWordsMax : 0);
+    const int need = L.bytes + (o.hot_cache > 0 ? 4 * dfqk::kHotWordsMax : 0);
     if (need > 227 * 1024)
         return fail(DFQ_EINVAL, "options need %d bytes of shared memory per block (max 232448)", need);
     return DFQ_OK;
@@ -373,8 +373,10 @@ int check_symmetric(dfq_graph* g) {
 }
 
 // Shared-memory words of the hot-vertex cache for a graph of bitmap_words.
+// hot_cache = K > 0: a cache of K KB (rounded down to 4 KB, at most 32 KB)
 int hot_words_for(const dfq_opts& o, int n) {
-    return o.hot_cache == 1 ? dfqk::hot_words_of(dfqk::kHotWordsMax, n) : 0;
+    const int words = dfqk::hot_limit_words(o.hot_cache);
+    return words > 0 ? dfqk::hot_words_of(words, n) : 0;
 }
 
 // Queue control-block reset + the cooperative kernel on g->stream.

@@ -376,7 +376,7 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     const void* fn = pick_single(o.block_threads, par);
     if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
     const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
-    const int hot = o.hot_cache == 1 ? hot_words_of(kHotWordsMax, p->n[graph]) : 0;
+    const int hot = hot_limit_words(o.hot_cache) > 0 ? hot_words_of(hot_limit_words(o.hot_cache), p->n[graph]) : 0;
     const int smem = lay.bytes + 4 * hot;
     int grid = 0;
     if ((rc = grid_for(p, fn, o.block_threads, smem, &grid))) return rc;
@@ -453,8 +453,8 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     // one cache size per pool (the largest graph's), so a captured launch
     // stays valid for any batch of the same shape
     int hot = 0;
-    if (o.hot_cache == 1)  // pools keep input ids: the cache only on request
-        for (int i = 0; i < p->ngraphs; ++i) hot = std::max(hot, hot_words_of(kHotWordsMax, p->n[i]));
+    if (hot_limit_words(o.hot_cache) > 0)  // the cache only on request
+        for (int i = 0; i < p->ngraphs; ++i) hot = std::max(hot, hot_words_of(hot_limit_words(o.hot_cache), p->n[i]));
     const int smem = lay.bytes + 4 * hot;
     int grid = 0, rc;
     if ((rc = grid_for(p, fn, o.block_threads, smem, &grid))) return rc;

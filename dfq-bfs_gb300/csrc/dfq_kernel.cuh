@@ -343,6 +343,13 @@ __device__ __forceinline__ bool group_barrier(Control* ctl, int gsize, unsigned&
 constexpr int kRing = 256;  // per-warp candidate ring (entries, power of two)
 constexpr int kHotWordsMax = 8192;  // hot-vertex visited cache: 32 KB, 262,144 vertices
 
+// Words of a hot-vertex cache of `kb` KB (0 if kb <= 0), rounded down to 4 KB,
+// at most kHotWordsMax.
+__host__ __device__ inline int hot_limit_words(int kb) {
+    const int w = kb > 0 ? (kb / 4) * 1024 : 0;
+    return w < kHotWordsMax ? w : kHotWordsMax;
+}
+
 // Hot-cache words for a graph of n vertices under a launch limit: whole
 // 32-word groups of the graph's bitmap (a multiple of 4 for 16-byte copies).
 __host__ __device__ inline int hot_words_of(int limit_words, int n) {

@@ -655,8 +655,9 @@ int dfq_server_create(dfq_pool* pool, const dfq_server_opts* opts, dfq_server** 
     s->fn = pick_serve(po.block_threads, par);
     if (!s->fn) { server_release_all(s); return fail(DFQ_EINVAL, "block_threads %d", po.block_threads); }
     s->hot_words = 0;
-    if (po.hot_cache == 1)  // pools keep input ids: the cache only on request
-        for (int i = 0; i < pool->ngraphs; ++i) s->hot_words = std::max(s->hot_words, hot_words_of(kHotWordsMax, pool->n[i]));
+    if (hot_limit_words(po.hot_cache) > 0)  // the cache only on request
+        for (int i = 0; i < pool->ngraphs; ++i)
+            s->hot_words = std::max(s->hot_words, hot_words_of(hot_limit_words(po.hot_cache), pool->n[i]));
     s->smem = smem_layout(po.block_threads, po.local_queue_cap, po.piece_edges, par).bytes + 4 * s->hot_words;
     S_TRY(grid_for(pool, s->fn, po.block_threads, s->smem, &s->grid));
     S_TRY(ensure_wide(pool, par));

@@ -147,11 +147,10 @@ typedef struct dfq_opts {
     int32_t timeout_ms;         /* bound on every device-side wait (0 = 5000) */
     int32_t wide_min_edges;     /* pools: a graph runs on the whole grid when it has at least */
     int32_t wide_min_degree;    /*   this many edges and this average degree (0 = defaults) */
-    int32_t hot_cache;          /* 1: on levels that probe, keep the visited bits of vertex ids
-                                   below 262,144 in 32 KB of shared memory per block (hub-first
-                                   ids put the most-probed vertices there); 0 or -1: no cache.
-                                   Off by default: measured slower on GB300 (its shared memory
-                                   comes out of L1 and each probe level refills it) */
+    int32_t hot_cache;          /* K in 1..32: on levels that probe, keep the visited bits of the
+                                   first K x 8192 vertex ids in K KB of shared memory per block
+                                   (K rounded down to 4 KB; hub-first ids put the most-probed
+                                   vertices there); 0 or -1: no cache (the default) */
     int32_t vertex_order;       /* read by dfq_graph_create only: 0 = hub-first ids (by
                                    descending degree) when the degrees are skewed, 1 = keep the
                                    input ids, 2 = hub-first always.  Results are always reported
