@@ -45,6 +45,7 @@ struct BatchParams {
     int medium_min, large_min, piece_edges, local_cap, local_budget, probe_first, use_tma;
     long long timeout_ns;
     int hot_words;  // hot-vertex cache words this launch reserves (0: none)
+    int reserve;    // blocks that run narrow queries during the wide phase
 };
 
 __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, int qi, const Workspace& ws) {
@@ -109,11 +110,16 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_batch_kernel(const __grid_con
     init_warp_barriers<B, PAR>(bp.local_cap, bp.piece_edges);
     WarpState ws{0u, false};
     if (blockIdx.x == 0 && threadIdx.x == 0) *bp.t0 = (long long)globaltimer();
-    for (int k = 0;; ++k) {
+    // the last `reserve` blocks skip the wide queries and start on the narrow
+    // ones (costliest first) at once, so the longest narrow runs overlap the
+    // wide phase instead of trailing it; the wide queries run on the others
+    const int wide_blocks = (int)gridDim.x - bp.reserve;
+    const bool in_wide = (int)blockIdx.x < wide_blocks;
+    for (int k = in_wide ? 0 : bp.n_wide;; ++k) {
         if (threadIdx.x == 0) {
             if (k < bp.n_wide) {
                 s_q = bp.wide_list[k];
-                s_gsize = (int)gridDim.x;
+                s_gsize = wide_blocks;
                 s_grank = (int)blockIdx.x;
                 fill_params(sp, bp, s_q, bp.wide_ws);
                 if (blockIdx.x == 0) bp.queries[s_q].t_start = (long long)globaltimer();
@@ -503,6 +509,9 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     bp.use_tma = o.use_tma;
     bp.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     bp.hot_words = hot;
+    // a sixteenth of the grid starts the narrow queries while the rest runs
+    // the wide ones (when there are both)
+    bp.reserve = (nw > 0 && nn > 0) ? std::min(nn, std::max(1, grid / 16)) : 0;
 
     auto enqueue = [&]() -> int {
         cudaError_t e1 = cudaMemcpyAsync(p->d_queries, p->h_queries, sizeof(BatchQuery) * nq, cudaMemcpyHostToDevice, p->stream);
