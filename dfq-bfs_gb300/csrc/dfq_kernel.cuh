@@ -922,7 +922,7 @@ __device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tall
 
 // Bottom-up level: every unvisited vertex v looks among its neighbours for
 // one at the current level; the first found becomes its parent.  A lane
-// checks its own vertex's first 32 neighbours (with hub-first ids the row's
+// checks its own vertices' first 32 neighbours (with hub-first ids the row's
 // hub comes first); lists still unresolved after that are finished by the
 // whole warp, 32 neighbours at a time.  Only v's lane writes v, so no claim
 // atomics are needed; levels are read through L2 (other blocks wrote this
@@ -932,52 +932,78 @@ template <bool PAR>
 __device__ __forceinline__ void bottom_up_level(const Params& p, const Lv& lv, Tally& t, int gwarp, int nwarps) {
     const int lane = threadIdx.x & 31;
     const int L = lv.next - 1;
-    for (int base = gwarp * 32; base < p.n; base += nwarps * 32) {
-        const int v = base + lane;
-        int s0 = 0, e0 = 0, par = -1;
-        bool open = false;
-        if (v < p.n && __ldcg(p.levels + v) == -1) {
-            s0 = __ldg(p.offsets + v);
-            e0 = __ldg(p.offsets + v + 1);
-            const int lim = min(e0, s0 + 32);
-            for (int k = s0; k < lim; ++k) {
+    // four vertices per lane: their first checks (own level, row bounds, the
+    // first neighbour - the row's hub - and its level) are in flight together
+    for (int base = gwarp * 128; base < p.n; base += nwarps * 128) {
+        int s0[4], e0[4], par[4], v[4];
+        unsigned unv = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            v[j] = base + j * 32 + lane;
+            s0[j] = e0[j] = 0;
+            par[j] = -1;
+            if (v[j] < p.n && __ldcg(p.levels + v[j]) == -1) unv |= 1u << j;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (unv >> j & 1) {
+                s0[j] = __ldg(p.offsets + v[j]);
+                e0[j] = __ldg(p.offsets + v[j] + 1);
+            }
+        int u0[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) u0[j] = ((unv >> j & 1) && e0[j] > s0[j]) ? __ldg(p.cols + s0[j]) : -1;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (u0[j] >= 0 && __ldcg(p.levels + u0[j]) == L) par[j] = u0[j];
+        unsigned open = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (!(unv >> j & 1) || par[j] >= 0) continue;
+            // the rest of the first 32 neighbours, one at a time
+            const int lim = min(e0[j], s0[j] + 32);
+            for (int k = s0[j] + 1; k < lim; ++k) {
                 const int u = __ldg(p.cols + k);
-                if (__ldcg(p.levels + u) == L) { par = u; break; }
+                if (__ldcg(p.levels + u) == L) { par[j] = u; break; }
             }
-            open = par < 0 && e0 > s0 + 32;
+            if (par[j] < 0 && e0[j] > s0[j] + 32) open |= 1u << j;
         }
-        unsigned rest = __ballot_sync(kFull, open);
-        while (rest) {  // long lists, one at a time with the whole warp
-            const int i = __ffs(rest) - 1;
-            rest &= rest - 1;
-            const int rs = __shfl_sync(kFull, s0, i) + 32, re = __shfl_sync(kFull, e0, i);
-            int got = -1;
-            for (int k0 = rs; k0 < re && got < 0; k0 += 32) {
-                const int k = k0 + lane;
-                const int u = k < re ? __ldg(p.cols + k) : -1;
-                const bool hit = u >= 0 && __ldcg(p.levels + u) == L;
-                const unsigned hm = __ballot_sync(kFull, hit);
-                if (hm) got = __shfl_sync(kFull, u, __ffs(hm) - 1);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            unsigned rest = __ballot_sync(kFull, open >> j & 1);
+            while (rest) {  // long lists, one at a time with the whole warp
+                const int i = __ffs(rest) - 1;
+                rest &= rest - 1;
+                const int rs = __shfl_sync(kFull, s0[j], i) + 32, re = __shfl_sync(kFull, e0[j], i);
+                int got = -1;
+                for (int k0 = rs; k0 < re && got < 0; k0 += 32) {
+                    const int k = k0 + lane;
+                    const int u = k < re ? __ldg(p.cols + k) : -1;
+                    const bool hit = u >= 0 && __ldcg(p.levels + u) == L;
+                    const unsigned hm = __ballot_sync(kFull, hit);
+                    if (hm) got = __shfl_sync(kFull, u, __ffs(hm) - 1);
+                }
+                if (lane == i) par[j] = got;
             }
-            if (lane == i) par = got;
         }
-        const bool found = par >= 0;
-        int st[4] = {0, 0, 0, 0}, dg[4] = {0, 0, 0, 0};
-        const int vv[4] = {v, 0, 0, 0};
+        int st[4], dg[4];
         unsigned loc = 0, lm = 0;
-        if (found) {
-            p.levels[v] = lv.next;
-            if (PAR) p.parents[v] = par;
-            atomicOr(&p.bitmap[v >> 5], 1u << (v & 31));
-            if (v < p.hub_n) p.hub_claim[v * kHubStride] = 1u << (v & 31);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            st[j] = dg[j] = 0;
+            if (par[j] < 0) continue;
+            p.levels[v[j]] = lv.next;
+            if (PAR) p.parents[v[j]] = par[j];
+            atomicOr(&p.bitmap[v[j] >> 5], 1u << (v[j] & 31));
+            if (v[j] < p.hub_n) p.hub_claim[v[j] * kHubStride] = 1u << (v[j] & 31);
             t.claims += 1;
             sh.claimed = 1;
-            st[0] = s0;
-            dg[0] = e0 - s0;
-            if (dg[0] >= p.large_min) lm = 1;
-            else if (dg[0] > 0) loc = 1;
+            st[j] = s0[j];
+            dg[j] = e0[j] - s0[j];
+            if (dg[j] >= p.large_min) lm |= 1u << j;
+            else if (dg[j] > 0) loc |= 1u << j;
         }
-        push_claims<PAR>(p, lv, loc, lm, st, dg, vv);
+        push_claims<PAR>(p, lv, loc, lm, st, dg, v);
     }
 }
 
