@@ -60,6 +60,10 @@ struct dfq_graph {
     int32_t* parents_int = nullptr;
     unsigned* hub_claim = nullptr;   // claim words of the first hub_n (new) ids
     int hub_n = 0;
+    // launch shape of the last launch (kernel, dynamic shared memory, blocks
+    // per SM cap) and the grid it gave: recomputed only when one changes
+    const void* cfg_kernel = nullptr;
+    int cfg_smem = -1, cfg_bps = -1, cfg_grid = 0;
 };
 
 namespace {
@@ -123,6 +127,16 @@ bool is_device_ptr(const void* p) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Device address of page-locked host memory mapped into the device's address
+// space (cudaHostAlloc / cudaHostRegister, e.g. a pinned torch tensor), else
+// null.  The kernel writes such output directly, so no separate copy follows.
+int32_t* host_mapped(int32_t* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return a.type == cudaMemoryTypeHost ? static_cast<int32_t*>(a.devicePointer) : nullptr;
 }
 
 __global__ void validate_csr_kernel(const int32_t* off, const int32_t* cols, int32_t n, int64_t e,
@@ -379,8 +393,11 @@ int hot_words_for(const dfq_opts& o, int n) {
     return words > 0 ? dfqk::hot_words_of(words, n) : 0;
 }
 
-// Queue control-block reset + the cooperative kernel on g->stream.
-int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
+// Queue control-block reset + the cooperative kernel on g->stream.  The
+// kernel computes into levels / parents (device); lv_host / pa_host, when
+// given, are mapped host buffers that its last pass writes the results to.
+int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int32_t* lv_host = nullptr,
+               int32_t* pa_host = nullptr) {
     const dfq_opts& o = g->opts;
     const bool par = parents != nullptr;
     KernelFn k = pick_kernel(o.block_threads, par);
@@ -388,12 +405,18 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
     const int hot_words = hot_words_for(o, g->n);
     const int smem = lay.bytes + 4 * hot_words;
-    CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    int per_sm = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k, o.block_threads, smem));
-    if (per_sm < 1) return fail(DFQ_EINVAL, "kernel does not fit on an SM with these options");
-    if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
-    const int grid = g->sms * per_sm;
+    if ((const void*)k != g->cfg_kernel || smem != g->cfg_smem || o.blocks_per_sm != g->cfg_bps) {
+        CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        int per_sm = 0;
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k, o.block_threads, smem));
+        if (per_sm < 1) return fail(DFQ_EINVAL, "kernel does not fit on an SM with these options");
+        if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
+        g->cfg_kernel = (const void*)k;
+        g->cfg_smem = smem;
+        g->cfg_bps = o.blocks_per_sm;
+        g->cfg_grid = g->sms * per_sm;
+    }
+    const int grid = g->cfg_grid;
 
     dfqk::Params p;
     memset(&p, 0, sizeof p);
@@ -436,12 +459,15 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
         p.src = g->rank_host[src];
         p.levels = g->levels_int;
         p.parents = par ? g->parents_int : nullptr;
-        p.levels_out = levels;
-        p.parents_out = parents;
+        p.levels_out = lv_host ? lv_host : levels;
+        p.parents_out = pa_host ? pa_host : parents;
         p.rank = g->rank;
         p.order = g->order;
         p.hub_claim = g->hub_claim;
         p.hub_n = g->hub_n;
+    } else {
+        p.levels_out = lv_host;
+        p.parents_out = pa_host;
     }
 
     CUDA_TRY(cudaMemsetAsync(g->ctl, 0, sizeof(dfqk::Control), g->stream));
@@ -450,8 +476,10 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents) {
     return DFQ_OK;
 }
 
-int fill_stats(dfq_graph* g, dfq_stats* st) {
-    CUDA_TRY(cudaMemcpyAsync(g->ctl_host, g->ctl, sizeof(dfqk::Control), cudaMemcpyDeviceToHost, g->stream));
+// Status and statistics of the last launch (full: the per-level traces too).
+int fill_stats(dfq_graph* g, dfq_stats* st, bool full = false) {
+    const size_t bytes = full ? sizeof(dfqk::Control) : offsetof(dfqk::Control, trace_ns);
+    CUDA_TRY(cudaMemcpyAsync(g->ctl_host, g->ctl, bytes, cudaMemcpyDeviceToHost, g->stream));
     CUDA_TRY(cudaStreamSynchronize(g->stream));
     const dfqk::Control& c = *g->ctl_host;
     if (st) {
@@ -655,7 +683,7 @@ int dfq_bfs_last_trace(dfq_graph* g, int64_t* start_ns, int32_t* frontier, int32
     if (!g || max_levels < 0 || (max_levels > 0 && (!start_ns || !frontier)))
         return fail(DFQ_EINVAL, "dfq_bfs_last_trace: bad arguments");
     DeviceGuard dg(g->device);
-    int rc = fill_stats(g, nullptr);
+    int rc = fill_stats(g, nullptr, true);
     if (rc) return rc;
     const dfqk::Control& c = *g->ctl_host;
     int n = std::min(std::min(max_levels, dfqk::kTraceLevels), c.stats.levels + 1);
@@ -671,7 +699,7 @@ int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels) {
     if (!g || max_levels < 0 || (max_levels > 0 && !out))
         return fail(DFQ_EINVAL, "dfq_bfs_last_levels: bad arguments");
     DeviceGuard dg(g->device);
-    int rc = fill_stats(g, nullptr);
+    int rc = fill_stats(g, nullptr, true);
     if (rc) return rc;
     const dfqk::Control& c = *g->ctl_host;
     int n = std::min(std::min(max_levels, dfqk::kTraceLevels), c.stats.levels + 1);
@@ -698,6 +726,10 @@ int dfq_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, dfq_st
     DeviceGuard dg(g->device);
     const bool lv_dev = is_device_ptr(levels);
     const bool pa_dev = parents && is_device_ptr(parents);
+    // pinned host outputs are written by the kernel itself; other host
+    // outputs are copied from device scratch after it
+    int32_t* lv_map = lv_dev ? nullptr : host_mapped(levels);
+    int32_t* pa_map = (parents && !pa_dev) ? host_mapped(parents) : nullptr;
     int32_t* dl = lv_dev ? levels : g->levels_tmp;
     int32_t* dp = nullptr;
     if (parents) {
@@ -711,12 +743,12 @@ int dfq_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, dfq_st
         }
     }
     CUDA_TRY(cudaEventRecord(g->ev0, g->stream));
-    int rc = launch_bfs(g, src, dl, dp);
+    int rc = launch_bfs(g, src, dl, dp, lv_map, pa_map);
     if (rc) return rc;
     CUDA_TRY(cudaEventRecord(g->ev1, g->stream));
-    if (!lv_dev)
+    if (!lv_dev && !lv_map)
         CUDA_TRY(cudaMemcpyAsync(levels, dl, sizeof(int32_t) * (size_t)g->n, cudaMemcpyDeviceToHost, g->stream));
-    if (parents && !pa_dev)
+    if (parents && !pa_dev && !pa_map)
         CUDA_TRY(cudaMemcpyAsync(parents, dp, sizeof(int32_t) * (size_t)g->n, cudaMemcpyDeviceToHost, g->stream));
     dfq_stats st;
     memset(&st, 0, sizeof st);

@@ -129,7 +129,8 @@ struct Params {
     // vertex order: when the graph was relabelled (rank != null) the kernel
     // runs on new ids, with levels / parents above indexed by new id, and at
     // the end writes levels_out[v] = levels[rank[v]] and parents_out[v] =
-    // order[parents[rank[v]]] for the caller's ids v
+    // order[parents[rank[v]]] for the caller's ids v.  Without rank, a
+    // non-null levels_out / parents_out (mapped host memory) gets a plain copy.
     const int* rank;
     const int* order;
     int* levels_out;
@@ -1420,18 +1421,19 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         }
     }
 
-    // ---- relabelled graph: levels (and parents) back to the caller's ids.
-    // Every block passed the final barrier after its last write, so all of
-    // them are visible here (read through L2).
-    if (ok && p.rank) {
+    // ---- results to the caller's buffers: on a relabelled graph levels (and
+    // parents) back to the caller's ids; otherwise a plain copy into mapped
+    // host memory.  Every block passed the final barrier after its last
+    // write, so all of them are visible here (read through L2).
+    if (ok && (p.levels_out || (PAR && p.parents_out))) {
         const long long gtid = (long long)grank * B + tid;
         const long long nth = (long long)gsize * B;
         for (long long v = gtid; v < p.n; v += nth) {
-            const int r = __ldg(p.rank + v);
-            p.levels_out[v] = __ldcg(p.levels + r);
-            if (PAR) {
+            const int r = p.rank ? __ldg(p.rank + v) : (int)v;
+            if (p.levels_out) p.levels_out[v] = __ldcg(p.levels + r);
+            if (PAR && p.parents_out) {
                 const int q = __ldcg(p.parents + r);
-                p.parents_out[v] = q >= 0 ? __ldg(p.order + q) : -1;
+                p.parents_out[v] = !p.order ? q : q >= 0 ? __ldg(p.order + q) : -1;
             }
         }
     }

@@ -280,6 +280,41 @@ def test_device_buffers_and_launch_api():
         assert st.edges == oracle.reached_edges(g.offsets, want)
 
 
+@pytest.mark.parametrize("order", [1, 2])
+def test_pinned_host_outputs(order):
+    """Pinned host outputs are written by the kernel's last pass (no separate
+    copy): levels and parents equal the pageable-buffer path's, with and
+    without hub-first ids, for levels alone, parents alone and both; the
+    statistics of a pinned run match too."""
+    torch = pytest.importorskip("torch")
+    g = d.gen_rmat(15, 16, seed=41)
+    with d.Graph(g, opts=opts(vertex_order=order)) as dg:
+        for s in g.pick_sources(3, seed=41):
+            s = int(s)
+            want = oracle.bfs(g.offsets, g.cols, s)
+            lv_h = torch.full((g.n,), 5, dtype=torch.int32).pin_memory()
+            pa_h = torch.full((g.n,), 5, dtype=torch.int32).pin_memory()
+            _, _, st = dg.bfs(s, levels_out=lv_h, parents_out=pa_h)
+            assert oracle.compare(want, lv_h.numpy())["mismatches"] == 0
+            assert oracle.validate_tree(g.offsets, g.cols, s, lv_h.numpy(), pa_h.numpy()) == 0
+            assert st.edges == oracle.reached_edges(g.offsets, want)
+            assert st.reached == int((want >= 0).sum())
+            # pinned levels with pageable parents, and the other way round
+            lv2 = torch.full((g.n,), 5, dtype=torch.int32).pin_memory()
+            pa2 = np.full(g.n, 5, np.int32)
+            dg.bfs(s, levels_out=lv2, parents_out=pa2)
+            assert torch.equal(lv2, lv_h)
+            assert oracle.validate_tree(g.offsets, g.cols, s, lv2.numpy(), pa2) == 0
+            lv3 = np.full(g.n, 5, np.int32)
+            pa3 = torch.full((g.n,), 5, dtype=torch.int32).pin_memory()
+            dg.bfs(s, levels_out=lv3, parents_out=pa3)
+            assert np.array_equal(lv3, lv_h.numpy())
+            assert oracle.validate_tree(g.offsets, g.cols, s, lv3, pa3.numpy()) == 0
+            lv4 = torch.full((g.n,), 5, dtype=torch.int32).pin_memory()
+            dg.bfs(s, levels_out=lv4)
+            assert torch.equal(lv4, lv_h)
+
+
 def test_invalid_source_and_csr():
     g = d.gen_rmat(8, 4, seed=1)
     with d.Graph(g) as dg:
