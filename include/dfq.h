@@ -208,7 +208,10 @@ int64_t dfq_graph_num_edges(const dfq_graph* g);
  * (DFQ:255-288: occupancy-sized cooperative launch of CUDA_BFS_KERNEL_CG_NEW,
  * events around launch + synchronize).  levels[n] (required) and parents[n]
  * (nullable) may be host or device pointers; parents[src] = src, parents of
- * unreached vertices = -1.  stats may be null. */
+ * unreached vertices = -1.  stats may be null.  Page-locked host buffers
+ * mapped into the device (cudaHostAlloc, cudaHostRegister) are written by the
+ * kernel itself at the end of the run; other host buffers are copied from
+ * device scratch after it. */
 int dfq_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, dfq_stats* stats);
 
 /* Queue the same BFS on the graph's stream and return at once (device
