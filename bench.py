@@ -582,6 +582,9 @@ def main():
            "clocks": ck.summary(),
            "per_bfs_ms_median": float(np.median(launch_ms)),
            "us_per_level": float(np.median(m["launch_ms"][0] * 1e3 / np.maximum(m["levels"], 1)))}
+    if cfg.get("symmetrized") or args.workload == "grid4096":
+        # Graph500 counts an undirected edge once: E_R / 2 on a symmetrised graph
+        out["graph500_gteps"] = value / 2
     if args.workload == "rmat22" and not args.no_do:
         out["direction_optimizing"] = direction_optimizing(g, srcs, er, levels, args, torch, d, pg)
     if rank == 0 and not args.no_cpu:
