@@ -594,7 +594,12 @@ def main():
         out["cpu_baseline"] = {"value": edges / tcpu / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
                                "sample": f"{nsrc} of the {len(srcs)} sources, serial oracle BFS, {tcpu:.1f} s"}
     if rank == 0 and not args.no_ref_gpu:
-        out["reference_gpu"] = reference_gpu(g, srcs, max_sources=16 if args.workload == "rmat22" else 2)
+        import oracle
+        k = 16 if args.workload == "rmat22" else 2
+        wants = [oracle.bfs(g.offsets, g.cols, int(s)) for s in srcs[:k]]
+        out["reference_gpu"] = reference_gpu(g, srcs, max_sources=k, wants=wants)
+        # the global-queue baseline of the reference's design space, on the first 4 of them
+        out["reference_gpu_global"] = reference_gpu(g, srcs, max_sources=min(4, k), kind="global", wants=wants)
     dg.close()
     if rank == 0 and args.workload == "rmat22" and not args.no_secondary:
         out["secondary"] = secondary_grid(torch, d, args)
@@ -640,25 +645,29 @@ def secondary_grid(torch, d, args):
     return res
 
 
-def reference_gpu(g, srcs, max_sources=16):
-    """The reference kernel on the same graph: median GTEPS over sources."""
+def reference_gpu(g, srcs, max_sources=16, kind="dfq", wants=None):
+    """The reference kernel on the same graph: median GTEPS over sources.
+    kind "dfq" = the shared-queue DFQ kernel, "global" = the global-queue
+    baseline; wants = oracle levels of the sources, if already computed."""
     try:
         import oracle
         from oracle import refgpu
     except Exception as e:  # pragma: no cover
         return {"unavailable": f"import failed: {e}"}
-    if not refgpu.available("dfq"):
+    if not refgpu.available(kind):
         return {"unavailable": "reference cubin not built (reference sources absent where build() ran)"}
-    res = {"kernel": "design/shared-q/atomic-sa/our-sep/upper-bound/bfs.cu", "sources": 0}
+    kernels = {"dfq": "design/shared-q/atomic-sa/our-sep/upper-bound/bfs.cu",
+               "global": "design/global-q/stripe-sa/gun-sep/lower-bound/bfs.cu"}
+    res = {"kernel": kernels[kind], "sources": 0}
     try:
-        with refgpu.RefGpu("dfq") as ref:
+        with refgpu.RefGpu(kind) as ref:
             ref.load(g.offsets, g.cols)
             gteps, ms, errors = [], [], 0
-            for s in srcs[:max_sources]:
-                want = oracle.bfs(g.offsets, g.cols, int(s))
+            for i, s in enumerate(srcs[:max_sources]):
+                want = wants[i] if wants is not None else oracle.bfs(g.offsets, g.cols, int(s))
                 ok, why = ref.safe_for(want)
                 if not ok:
-                    return {"unavailable": f"refused (queue bounds): {why}"}
+                    return {"kernel": kernels[kind], "unavailable": f"refused (queue bounds): {why}"}
                 ref.bfs(int(s))  # warm
                 lv, t = ref.bfs(int(s))
                 errors += oracle.compare(want, lv)["near_errors"]
@@ -671,7 +680,7 @@ def reference_gpu(g, srcs, max_sources=16):
                         "gteps_aggregate": float(sum(g_ * m for g_, m in zip(gteps, ms)) / sum(ms)),
                         "errors": int(errors), "grid": ref.grid})
     except Exception as e:
-        return {"unavailable": f"{type(e).__name__}: {e}"}
+        return {"kernel": kernels[kind], "unavailable": f"{type(e).__name__}: {e}"}
     return res
 
 
