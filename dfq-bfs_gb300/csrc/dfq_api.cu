@@ -129,14 +129,16 @@ bool is_device_ptr(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// Device address of page-locked host memory mapped into the device's address
-// space (cudaHostAlloc / cudaHostRegister, e.g. a pinned torch tensor), else
-// null.  The kernel writes such output directly, so no separate copy follows.
-int32_t* host_mapped(int32_t* p) {
+// Device address of page-locked host memory mapped into device dev's address
+// space (cudaHostAlloc / cudaHostRegister on that device, e.g. a pinned torch
+// tensor), else null.  The kernel writes such output directly, so no separate
+// copy follows; memory pinned through another device is copied instead.
+int32_t* host_mapped(int32_t* p, int dev) {
     if (!p) return nullptr;
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
-    return a.type == cudaMemoryTypeHost ? static_cast<int32_t*>(a.devicePointer) : nullptr;
+    if (a.type != cudaMemoryTypeHost || a.device != dev) return nullptr;
+    return static_cast<int32_t*>(a.devicePointer);
 }
 
 __global__ void validate_csr_kernel(const int32_t* off, const int32_t* cols, int32_t n, int64_t e,
@@ -728,8 +730,8 @@ int dfq_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, dfq_st
     const bool pa_dev = parents && is_device_ptr(parents);
     // pinned host outputs are written by the kernel itself; other host
     // outputs are copied from device scratch after it
-    int32_t* lv_map = lv_dev ? nullptr : host_mapped(levels);
-    int32_t* pa_map = (parents && !pa_dev) ? host_mapped(parents) : nullptr;
+    int32_t* lv_map = lv_dev ? nullptr : host_mapped(levels, g->device);
+    int32_t* pa_map = (parents && !pa_dev) ? host_mapped(parents, g->device) : nullptr;
     int32_t* dl = lv_dev ? levels : g->levels_tmp;
     int32_t* dp = nullptr;
     if (parents) {
