@@ -100,6 +100,7 @@ int validate_opts(const dfq_opts& o) {
     if (o.hot_cache < -1 || o.hot_cache > 32) return fail(DFQ_EINVAL, "hot_cache must be -1, 0 or 1..32 (KB)");
     if (o.profile != 0 && o.profile != 1) return fail(DFQ_EINVAL, "profile must be 0 or 1");
     if (o.direction != 0 && o.direction != 1) return fail(DFQ_EINVAL, "direction must be 0 or 1");
+    if (o.stall_test_level < 0) return fail(DFQ_EINVAL, "stall_test_level must be >= 0");
     if (o.vertex_order < 0 || o.vertex_order > 2) return fail(DFQ_EINVAL, "vertex_order must be 0, 1 or 2");
     const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true);
     const int need = L.bytes + (o.hot_cache > 0 ? 4 * dfqk::kHotWordsMax : 0);
@@ -452,6 +453,7 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
     if (o.direction == 1 && !g->symmetric)
         return fail(DFQ_EINVAL, "direction = 1 needs a graph created with direction = 1 (checked undirected)");
     p.direction = o.direction;
+    p.stall_level = o.stall_test_level;
     p.e = (int)g->e;
     if (g->relabeled) {
         if (par && !g->parents_int) {
@@ -531,6 +533,7 @@ void dfq_opts_default(dfq_opts* o) {
     o->vertex_order = 0;
     o->profile = 0;
     o->direction = 0;
+    o->stall_test_level = 0;
 }
 
 int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int64_t e, const dfq_opts* opts,

@@ -140,6 +140,9 @@ struct Params {
     unsigned* hub_claim;
     int hub_n;
     int map_src;  // 1: src is an input id, renumbered here through rank
+    // failure-path test hook: k > 0 = at the end of level k-1 the group's last
+    // block skips its barrier arrival, so every block's bounded wait runs out
+    int stall_level;
 };
 
 // Hub claim words sit a 32-byte sector apart: with hub-first ids ~1000 hubs
@@ -269,12 +272,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 // global memory.  Returns false (all threads of the block) if the wait timed
 // out or another block reported an error.
 __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, long long timeout_ns,
-                                             int* s_flag, const LevelCtr* next, int* s_in, int gsize) {
+                                             int* s_flag, const LevelCtr* next, int* s_in, int gsize,
+                                             bool skip_arrive = false) {
     __syncthreads();
     if (threadIdx.x == 0) {
         target += (unsigned)gsize;
         int ok = 1;
-        red_add_release(&ctl->barrier, 1u);
+        if (!skip_arrive) red_add_release(&ctl->barrier, 1u);
         unsigned long long t0 = 0;
         for (unsigned it = 0;; ++it) {
             unsigned cur = ld_acquire(&ctl->barrier);
@@ -316,8 +320,9 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
 // level's input into s_in from the block's own shared tallies (they are the
 // whole group's), so the barrier is just the block barrier.
 __device__ __forceinline__ bool group_barrier(Control* ctl, int gsize, unsigned& target, long long timeout_ns,
-                                              int* s_flag, const LevelCtr* next, int* s_in, bool local_in) {
-    if (gsize > 1) return grid_barrier(ctl, target, timeout_ns, s_flag, next, s_in, gsize);
+                                              int* s_flag, const LevelCtr* next, int* s_in, bool local_in,
+                                              bool skip_arrive = false) {
+    if (gsize > 1) return grid_barrier(ctl, target, timeout_ns, s_flag, next, s_in, gsize, skip_arrive);
     if (local_in) {
         __syncthreads();
         return s_block_err == 0;
@@ -1409,7 +1414,8 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             sh.ovf_edges = sh.large_edges = 0;
         }
         cur ^= 1;
-        ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in, true);
+        ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in, true,
+                           p.stall_level == L + 1 && grank == gsize - 1);
         if (p.profile && tid == 0 && L < kTraceLevels) {
             // recorded after the barrier: its release would otherwise wait for them
             atomicMax(&ctl->trace_done_last[L], done_ns);

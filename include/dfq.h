@@ -164,6 +164,11 @@ typedef struct dfq_opts {
                                    dfq_graph_create, which checks that every row is sorted and
                                    every edge u->v has its v->u (else DFQ_EINVAL).  Same levels;
                                    parents may differ (still a BFS tree); E_R still reported. */
+    int32_t stall_test_level;   /* failure-path test hook, 0 = off (the default).  k > 0: at the
+                                   end of level k-1 the launch's last block does not arrive at the
+                                   grid barrier, so every block's bounded wait runs out after
+                                   timeout_ms and the call returns DFQ_ETIMEOUT; the graph stays
+                                   usable.  Single-source launches (dfq_bfs, dfq_bfs_launch) only. */
 } dfq_opts;
 
 typedef struct dfq_stats {

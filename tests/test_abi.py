@@ -22,6 +22,23 @@ def test_header_and_binding_agree():
     assert sorted(d.EXPORTS) == declared_functions()
 
 
+def struct_fields(name):
+    """Field names of `typedef struct name {...} name;` in dfq.h, in order."""
+    text = (ROOT / "include" / "dfq.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), text, flags=re.S).group(1)
+    return re.findall(r"\b(?:u?int(?:8|16|32|64)_t|double|float)\s+(\w+)\s*;", body)
+
+
+def test_option_struct_layout_matches_header():
+    """The ctypes mirror of dfq_opts has the header's int32 fields in the
+    header's order (a mismatch would shift every option after it)."""
+    assert [f for f, _ in d.Opts._fields_] == struct_fields("dfq_opts")
+    assert all(t is C.c_int32 for _, t in d.Opts._fields_)
+    o = d.default_opts()
+    assert o.stall_test_level == 0 and o.direction == 0 and o.timeout_ms == 5000
+
+
 def test_library_exports_every_declared_symbol():
     L = d.lib()
     for name in declared_functions():

@@ -315,6 +315,36 @@ def test_pinned_host_outputs(order):
             assert torch.equal(lv4, lv_h)
 
 
+@pytest.mark.parametrize("level", [1, 2])
+def test_barrier_timeout_reported_and_graph_usable(level):
+    """Failure path without a fault: with stall_test_level the last block
+    skips one grid-barrier arrival, so every block's bounded wait runs out
+    after timeout_ms; the call returns ETIMEOUT (through dfq_bfs and through
+    dfq_bfs_launch + sync) and the same graph then runs exact BFS again."""
+    import time
+    torch = pytest.importorskip("torch")
+    g = d.gen_rmat(14, 8, seed=12)
+    src = int(g.pick_sources(1, seed=12)[0])
+    assert oracle.bfs(g.offsets, g.cols, src).max() >= level  # the stalled barrier is reached
+    with d.Graph(g, opts=opts(timeout_ms=20)) as dg:
+        dg.set_opts({"stall_test_level": level})
+        t0 = time.perf_counter()
+        with pytest.raises(d.DfqError) as e:
+            dg.bfs(src)
+        assert e.value.name == "ETIMEOUT" and "barrier" in str(e.value)
+        assert time.perf_counter() - t0 < 5.0
+        lv = torch.full((g.n,), 3, dtype=torch.int32, device="cuda")
+        dg.launch(src, lv)
+        with pytest.raises(d.DfqError) as e:
+            dg.sync()
+        assert e.value.name == "ETIMEOUT"
+        dg.set_opts({"stall_test_level": 0})
+        run_and_check(g, src, graph=dg)
+        dg.launch(src, lv)
+        dg.sync()
+        assert oracle.compare(oracle.bfs(g.offsets, g.cols, src), lv.cpu().numpy())["mismatches"] == 0
+
+
 def test_invalid_source_and_csr():
     g = d.gen_rmat(8, 4, seed=1)
     with d.Graph(g) as dg:
