@@ -57,6 +57,17 @@ int build_csr(const std::vector<EdgeSpan>& spans, int32_t n, int32_t flags, dfq_
 int hub_first_csr(const dfq_csr& in, int mode, dfq_csr* out, std::vector<int32_t>* rank,
                   std::vector<int32_t>* order);
 
+// Set kernel fn's dynamic shared-memory limit to what the next launch needs.
+// The limit is a property of the function, shared by every graph, pool and
+// entry point launching it, so it is set right before each launch (never
+// cached per caller: another caller may have set a smaller value since).
+int allow_dyn_smem(const void* fn, int smem_needed);
+
+// The single-source kernel dfqk::dfq_bfs_kernel<block_threads, par>, compiled
+// once (in dfq_api.cu) and launched through this handle by every entry point
+// that runs one BFS on a whole cooperative grid; null for an unsupported size.
+const void* single_source_kernel(int block_threads, bool par);
+
 // Run body(i) for i in [0, t) on t threads (the caller's thread takes i = 0).
 template <class F>
 void run_threads(int t, F&& body) {

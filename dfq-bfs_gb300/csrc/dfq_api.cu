@@ -61,7 +61,8 @@ struct dfq_graph {
     unsigned* hub_claim = nullptr;   // claim words of the first hub_n (new) ids
     int hub_n = 0;
     // launch shape of the last launch (kernel, dynamic shared memory, blocks
-    // per SM cap) and the grid it gave: recomputed only when one changes
+    // per SM cap) and the occupancy grid it gave: recomputed only when one
+    // changes (the kernel's shared-memory limit is still set every launch)
     const void* cfg_kernel = nullptr;
     int cfg_smem = -1, cfg_bps = -1, cfg_grid = 0;
 };
@@ -408,8 +409,9 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
     const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
     const int hot_words = hot_words_for(o, g->n);
     const int smem = lay.bytes + 4 * hot_words;
+    // the limit is shared with every other caller of this kernel: set it each time
+    if (int rc = allow_dyn_smem((const void*)k, smem)) return rc;
     if ((const void*)k != g->cfg_kernel || smem != g->cfg_smem || o.blocks_per_sm != g->cfg_bps) {
-        CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         int per_sm = 0;
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k, o.block_threads, smem));
         if (per_sm < 1) return fail(DFQ_EINVAL, "kernel does not fit on an SM with these options");
@@ -511,6 +513,18 @@ struct DeviceGuard {
 };
 
 }  // namespace
+
+namespace dfq {
+int allow_dyn_smem(const void* fn, int smem_needed) {
+    cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_needed);
+    if (err != cudaSuccess) return fail(DFQ_ECUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(err));
+    return DFQ_OK;
+}
+
+const void* single_source_kernel(int block_threads, bool par) {
+    return (const void*)pick_kernel(block_threads, par);
+}
+}  // namespace dfq
 
 extern "C" {
 

@@ -201,15 +201,6 @@ void* pick_batch(int B, bool par) {
         default: return nullptr;
     }
 }
-void* pick_single(int B, bool par) {
-    switch (B) {
-        case 256: return par ? (void*)dfq_bfs_kernel<256, true> : (void*)dfq_bfs_kernel<256, false>;
-        case 512: return par ? (void*)dfq_bfs_kernel<512, true> : (void*)dfq_bfs_kernel<512, false>;
-        case 1024: return par ? (void*)dfq_bfs_kernel<1024, true> : (void*)dfq_bfs_kernel<1024, false>;
-        default: return nullptr;
-    }
-}
-
 int launch_coop(const void* fn, int grid, int B, int smem, void* arg, cudaStream_t s) {
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof cfg);
@@ -379,7 +370,7 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     int rc = ensure_wide(p, par);
     if (rc) return rc;
     const dfq_opts& o = p->opts;
-    const void* fn = pick_single(o.block_threads, par);
+    const void* fn = single_source_kernel(o.block_threads, par);
     if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
     const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
     const int hot = hot_limit_words(o.hot_cache) > 0 ? hot_words_of(hot_limit_words(o.hot_cache), p->n[graph]) : 0;

@@ -102,17 +102,15 @@ int setup_device(int dev, const dfq_opts& o, DeviceSetup** out) {
         err = cudaGetDeviceProperties(&prop, dev);
         if (err != cudaSuccess) return fail(DFQ_ECUDA, "dfq_bfs_noalloc: %s", cudaGetErrorString(err));
         if (!prop.cooperativeLaunch) return fail(DFQ_ECUDA, "dfq_bfs_noalloc: no cooperative launch on device %d", dev);
-        const void* fns[2] = {(const void*)dfqk::dfq_bfs_kernel<kBlock, false>,
-                              (const void*)dfqk::dfq_bfs_kernel<kBlock, true>};
+        const void* fns[2] = {single_source_kernel(kBlock, false), single_source_kernel(kBlock, true)};
         for (int i = 0; i < 2; ++i) {
             // input ids are kept here, so the hot-vertex cache stays off (as
             // hot_cache = 0 leaves it for graphs not given hub-first ids)
             const dfqk::SmemLayout lay = dfqk::smem_layout(kBlock, o.local_queue_cap, o.piece_edges, i == 1);
             d.smem[i] = lay.bytes;
-            err = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, d.smem[i]);
+            if (int rc = allow_dyn_smem(fns[i], d.smem[i])) return rc;
             int per_sm = 0;
-            if (err == cudaSuccess)
-                err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], kBlock, d.smem[i]);
+            err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fns[i], kBlock, d.smem[i]);
             if (err != cudaSuccess || per_sm < 1)
                 return fail(DFQ_ECUDA, "dfq_bfs_noalloc: kernel setup failed: %s", cudaGetErrorString(err));
             d.grid[i] = prop.multiProcessorCount * per_sm;
@@ -192,7 +190,9 @@ extern "C" int dfq_bfs_noalloc(const int32_t* offsets, const int32_t* cols, int3
     p.use_tma = o.use_tma;
     p.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     const bool par = parents != nullptr;
-    const void* fn = par ? (const void*)dfqk::dfq_bfs_kernel<kBlock, true> : (const void*)dfqk::dfq_bfs_kernel<kBlock, false>;
+    const void* fn = single_source_kernel(kBlock, par);
+    // the kernel is shared with the graph handles, which set its limit too
+    if (int rc = allow_dyn_smem(fn, ds->smem[par ? 1 : 0])) return rc;
     void* args[] = {&p};
     if ((err = cudaMemsetAsync(ctl, 0, sizeof(dfqk::Control), s)) != cudaSuccess ||
         (err = cudaLaunchCooperativeKernel(fn, dim3(ds->grid[par ? 1 : 0]), dim3(kBlock), args, ds->smem[par ? 1 : 0], s)) !=

@@ -219,9 +219,9 @@ inline int ensure_wide(dfq_pool* p, bool par) {
 }
 
 inline int grid_for(dfq_pool* p, const void* fn, int B, int smem, int* grid) {
-    cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (int rc = allow_dyn_smem(fn, smem)) return rc;
     int per_sm = 0;
-    if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B, smem);
+    cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, B, smem);
     if (err != cudaSuccess || per_sm < 1)
         return fail(DFQ_ECUDA, "kernel does not fit: %s", cudaGetErrorString(err));
     if (p->opts.blocks_per_sm > 0) per_sm = std::min(per_sm, p->opts.blocks_per_sm);

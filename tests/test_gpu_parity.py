@@ -345,6 +345,32 @@ def test_barrier_timeout_reported_and_graph_usable(level):
         assert oracle.compare(oracle.bfs(g.offsets, g.cols, src), lv.cpu().numpy())["mismatches"] == 0
 
 
+def test_graphs_needing_different_shared_memory_alternate():
+    """The single-source kernel is one function shared by every graph handle
+    and by the no-alloc entry point: handles whose layouts need different
+    shared memory (a 32 KB hot cache, the smallest pieces) alternate on one
+    device, with no-alloc runs in between, and every run stays exact."""
+    torch = pytest.importorskip("torch")
+    g = d.gen_rmat(14, 16, seed=5)
+    src = int(g.pick_sources(1, seed=5)[0])
+    want = oracle.bfs(g.offsets, g.cols, src)
+    off = torch.from_numpy(g.offsets).cuda()
+    cols = torch.from_numpy(g.cols).cuda()
+    big = d.Graph(g, opts=opts(hot_cache=32, vertex_order=2))
+    small = d.Graph(g, opts=opts(piece_edges=64, large_min_degree=64))
+    try:
+        for _ in range(2):
+            for dg in (big, small):
+                run_and_check(g, src, graph=dg)
+                lv = torch.full((g.n,), 9, dtype=torch.int32, device="cuda")
+                d.bfs_noalloc(off, cols, g.n, g.e, src, lv)
+                torch.cuda.synchronize()
+                assert oracle.compare(want, lv.cpu().numpy())["mismatches"] == 0
+    finally:
+        big.close()
+        small.close()
+
+
 def test_invalid_source_and_csr():
     g = d.gen_rmat(8, 4, seed=1)
     with d.Graph(g) as dg:
