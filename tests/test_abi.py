@@ -30,6 +30,11 @@ def struct_fields(name):
     return re.findall(r"\b(?:u?int(?:8|16|32|64)_t|double|float)\s+(\w+)\s*;", body)
 
 
+MIRRORS = {"dfq_csr": "_Csr", "dfq_opts": "Opts", "dfq_stats": "Stats", "dfq_level_info": "LevelInfo",
+           "dfq_query": "Query", "dfq_query_result": "QueryResult", "dfq_server_opts": "ServerOpts",
+           "dfq_server_result": "ServerResult"}
+
+
 def test_option_struct_layout_matches_header():
     """The ctypes mirror of dfq_opts has the header's int32 fields in the
     header's order (a mismatch would shift every option after it)."""
@@ -37,6 +42,34 @@ def test_option_struct_layout_matches_header():
     assert all(t is C.c_int32 for _, t in d.Opts._fields_)
     o = d.default_opts()
     assert o.stall_test_level == 0 and o.direction == 0 and o.timeout_ms == 5000
+
+
+def test_struct_mirrors_match_the_c_layout(tmp_path):
+    """Every struct the binding mirrors has the C compiler's size and field
+    offsets (a C program built against dfq.h prints them)."""
+    import shutil
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "dfq.h"', "int main(void) {"]
+    for cname, pyname in MIRRORS.items():
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for f, _ in getattr(d, pyname)._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, f"-I{ROOT / 'include'}", str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        cname, f, v = line.split()
+        got[(cname, f)] = int(v)
+    for cname, pyname in MIRRORS.items():
+        cls = getattr(d, pyname)
+        assert C.sizeof(cls) == got[(cname, "sizeof")], cname
+        for f, _ in cls._fields_:
+            assert getattr(cls, f).offset == got[(cname, f)], (cname, f)
 
 
 def test_library_exports_every_declared_symbol():
