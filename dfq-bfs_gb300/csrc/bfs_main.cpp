@@ -42,9 +42,12 @@ bool is_int_prefix(const char* s) { return is_int(s) && strlen(s) < 11; }
 void usage() {
     fprintf(stderr,
             "usage: bfs <graph> [source] [--ref-compat] [--symmetrize] [--parents] [--no-check]\n"
-            "           [--repeat K] [--autotune] [--json] [--save-bin PATH] [--opt NAME=VALUE]... [$]\n"
+            "           [--repeat K] [--autotune] [--json] [--save-bin PATH] [--opt NAME=VALUE]...\n"
+            "           [--frontier-profile [--profile-tiles A,B,C,E] [--profile-grid BLOCKS]] [$]\n"
             "  --opt sets one field of dfq_opts (include/dfq.h), e.g. --opt probe_first=0;\n"
-            "  the reference's design variants are separate programs, here they are options\n");
+            "  the reference's design variants are separate programs, here they are options\n"
+            "  --frontier-profile prints the reference profiler's idle lanes per level and bin\n"
+            "  (bfs_ftr_prof.cu; tiles default 16,128,1024,8192, grid 304 blocks of 1024)\n");
 }
 
 // dfq_opts fields settable with --opt NAME=VALUE.
@@ -102,6 +105,9 @@ int main(int argc, char** argv) {
          autotune = false;
     int repeat = 1;
     const char* save_bin = nullptr;
+    bool frontier_profile = false;
+    int32_t prof_tiles[4] = {16, 128, 1024, 8192};  // the reference profiler's TILE_SIZ_A/B/C/E
+    int32_t prof_grid = 304;                          // its occupancy-sized grid on GB300 (x 1024 threads)
     long long src_arg = -1;
     const bool interactive = argv[argc - 1][0] == '$';
     dfq_opts opts;
@@ -117,6 +123,23 @@ int main(int argc, char** argv) {
         else if (!strcmp(a, "--autotune")) autotune = true;
         else if (!strcmp(a, "--repeat") && i + 1 < argc) repeat = atoi(argv[++i]);
         else if (!strcmp(a, "--save-bin") && i + 1 < argc) save_bin = argv[++i];
+        else if (!strcmp(a, "--frontier-profile")) frontier_profile = true;
+        else if (!strcmp(a, "--profile-tiles") && i + 1 < argc) {
+            int t[4];
+            char tail = 0;
+            bool ok = sscanf(argv[++i], "%d,%d,%d,%d%c", &t[0], &t[1], &t[2], &t[3], &tail) == 4;
+            for (int k = 0; ok && k < 4; ++k)
+                ok = t[k] > 0 && (t[k] & (t[k] - 1)) == 0 && (k == 0 || t[k] > t[k - 1]);
+            if (!ok) {
+                fprintf(stderr, "bfs: --profile-tiles '%s': need four increasing powers of two A,B,C,E\n", argv[i]);
+                return 2;
+            }
+            for (int k = 0; k < 4; ++k) prof_tiles[k] = t[k];
+        }
+        else if (!strcmp(a, "--profile-grid") && i + 1 < argc) {
+            prof_grid = atoi(argv[++i]);
+            if (prof_grid < 1) { fprintf(stderr, "bfs: --profile-grid needs a block count >= 1\n"); return 2; }
+        }
         else if (!strcmp(a, "--opt") && i + 1 < argc) {
             if (!set_opt(opts, argv[++i])) {
                 fprintf(stderr, "bfs: --opt '%s': not NAME=INTEGER with a dfq_opts field name\n", argv[i]);
@@ -209,6 +232,28 @@ int main(int argc, char** argv) {
             }
         }
         const int64_t errors = near_errors + extra + tree_bad;
+        if (frontier_profile) {
+            // the reference profiler's block (bfs_ftr_prof.cu:110-114,206-208), before the result
+            // lines so that "- Time" stays the second-to-last token
+            const int64_t threads = (int64_t)prof_grid * 1024;
+            const int32_t max_levels = st.depth + 1;
+            std::vector<int64_t> idle((size_t)max_levels * 5), count((size_t)max_levels * 5);
+            const int k = dfq_frontier_profile(&g, levels.data(), prof_tiles, threads, max_levels, idle.data(),
+                                               count.data());
+            if (k < 0) {
+                fprintf(stderr, "bfs: frontier profile: %s\n", dfq_last_error());
+                status = 1;
+            } else {
+                printf("Dim: %d %d\n", prof_grid, 1024);
+                printf("Siz: %d %d %d %d %lld\n", prof_tiles[0], prof_tiles[1], prof_tiles[2], prof_tiles[3],
+                       (long long)threads);
+                printf("Rng: %d %d %d %d inf\n", prof_tiles[0], prof_tiles[1], prof_tiles[2], prof_tiles[3]);
+                for (int l = 0; l < k; ++l)
+                    printf("%d: %lld %lld %lld %lld %lld\n", l, (long long)idle[(size_t)l * 5],
+                           (long long)idle[(size_t)l * 5 + 1], (long long)idle[(size_t)l * 5 + 2],
+                           (long long)idle[(size_t)l * 5 + 3], (long long)idle[(size_t)l * 5 + 4]);
+            }
+        }
         printf("- Dist  = %d\n", dist);
         printf("- Touch = %g %% (%lld / %d)\n", (double)near_nodes / (double)g.n * 100, (long long)near_nodes, g.n);
         if (errors) printf("- Error = \033[31m%lld\033[0;1m\n", (long long)errors);

@@ -41,7 +41,7 @@ EXPORTS = [
     "dfq_pool_create", "dfq_pool_destroy", "dfq_pool_num_graphs", "dfq_pool_graph_info", "dfq_pool_bfs",
     "dfq_pool_batch", "dfq_server_create", "dfq_server_submit", "dfq_server_poll", "dfq_server_levels",
     "dfq_server_release", "dfq_server_pending", "dfq_server_destroy", "dfq_server_replay",
-    "dfq_set_host_threads", "dfq_host_threads", "dfq_bfs_last_levels",
+    "dfq_set_host_threads", "dfq_host_threads", "dfq_bfs_last_levels", "dfq_frontier_profile",
 ]
 BATCH_GRAPH = 1
 
@@ -135,6 +135,8 @@ def lib() -> C.CDLL:
     L.dfq_gen_grid.argtypes = [C.c_int32, C.c_double, C.c_uint64, C.c_int32, C.POINTER(_Csr),
                                C.POINTER(P32)]
     L.dfq_pick_sources.argtypes = [C.POINTER(_Csr), C.c_int32, C.c_uint64, P32]
+    L.dfq_frontier_profile.argtypes = [C.POINTER(_Csr), P32, P32, C.c_int64, C.c_int32,
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.dfq_free.argtypes = [C.c_void_p]
     L.dfq_free.restype = None
     L.dfq_opts_default.argtypes = [C.POINTER(Opts)]
@@ -258,6 +260,34 @@ def set_host_threads(threads: int) -> None:
 
 def host_threads() -> int:
     return int(lib().dfq_host_threads())
+
+
+REF_PROFILE_TILES = (16, 128, 1024, 8192)  # TILE_SIZ_A/B/C/E of the reference's frontier profiler
+
+
+def frontier_profile(g: "Csr", levels, tiles=REF_PROFILE_TILES, threads: int = 304 * 1024,
+                     max_levels: int | None = None):
+    """Idle lanes and frontier counts per level and bin of the reference's
+    binned expansion (dfq_frontier_profile): two int64 arrays of shape
+    (levels, 5), bins = degree <= tiles[0..3], then the whole-grid bin.
+    threads = the reference launch's gridDim.x * blockDim.x (its
+    occupancy-sized grid on GB300 is 304 blocks of 1024)."""
+    lv = np.ascontiguousarray(levels, dtype=np.int32)
+    if lv.shape != (g.n,):
+        raise ValueError("levels must hold one entry per vertex")
+    t = np.ascontiguousarray(tiles, dtype=np.int32)
+    if t.shape != (4,):
+        raise ValueError("tiles must be four sizes")
+    m = int(max(int(lv.max(initial=-1)) + 1, 0) if max_levels is None else max_levels)
+    idle = np.zeros((max(m, 1), 5), np.int64)
+    cnt = np.zeros((max(m, 1), 5), np.int64)
+    c = g._as_c()
+    k = lib().dfq_frontier_profile(C.byref(c), _p32(lv), _p32(t), int(threads), m,
+                                   idle.ctypes.data_as(C.POINTER(C.c_int64)),
+                                   cnt.ctypes.data_as(C.POINTER(C.c_int64)))
+    if k < 0:
+        check(k)
+    return idle[:k], cnt[:k]
 
 
 def load(path: str | os.PathLike, fmt: str = "auto", flags: int = 0) -> Csr:

@@ -26,7 +26,7 @@ CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-un
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
                   "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
 
-HOST_SRCS = ["host_graph.cpp", "host_gen.cpp", "autotune.cpp"]
+HOST_SRCS = ["host_graph.cpp", "host_gen.cpp", "autotune.cpp", "host_profile.cpp"]
 CUDA_SRCS = ["dfq_api.cu", "dfq_noalloc.cu", "dfq_batch.cu", "dfq_serve.cu"]
 HEADERS = ["common.hpp", "dfq_kernel.cuh", "dfq_pool.cuh"]
 

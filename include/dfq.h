@@ -261,6 +261,24 @@ typedef struct dfq_level_info {
 } dfq_level_info;
 int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels);
 
+/* Idle-lane profile of the reference's binned expansion for one BFS,
+ * computed exactly on the host from its levels (identical to the
+ * reference's) and the degrees.  Replaces the device counters of
+ * design/shared-q/atomic-sa/our-sep/upper-bound/bfs_ftr_prof.cu:98-144 (its
+ * "L: a b c e f" lines, printed at :206-208).  A frontier vertex of level L
+ * with degree d > 0 falls in the first bin whose range holds d (d <=
+ * tiles[0], tiles[1], tiles[2], tiles[3], else the fifth, whole-grid bin);
+ * count[L][bin] += 1 and idle[L][bin] += tile - (d & (tile - 1)) for the
+ * four tiled bins, threads - (d % threads) for the fifth - the reference's
+ * formula, which also charges a whole tile when d is a multiple of it.
+ * tiles: four increasing powers of two (the reference's TILE_SIZ_A/B/C/E,
+ * bfs_ftr_prof.cu:18-35, e.g. 16, 128, 1024, 8192); threads: its
+ * gridDim.x * blockDim.x.  idle and count hold max_levels x 5 entries (either
+ * may be null).  Returns the number of levels filled (depth + 1, at most
+ * max_levels) or a negative status. */
+int dfq_frontier_profile(const dfq_csr* g, const int32_t* levels, const int32_t tiles[4], int64_t threads,
+                         int32_t max_levels, int64_t* idle, int64_t* count);
+
 /* Choose opts for this graph by timing candidate settings on a few sources;
  * writes the winner to *best and installs it on the graph. */
 int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, dfq_opts* best);

@@ -105,3 +105,9 @@ def test_bfs_program_usage():
     assert r.returncode == 2 and "usage" in r.stderr
     r = subprocess.run([str(exe), "/nonexistent.dat"], capture_output=True, text=True)
     assert r.returncode == 1 and "cannot open" in r.stderr
+    # profile options are checked before anything is loaded
+    r = subprocess.run([str(exe), "/nonexistent.dat", "--frontier-profile", "--profile-tiles", "16,100,1024,8192"],
+                       capture_output=True, text=True)
+    assert r.returncode == 2 and "powers of two" in r.stderr
+    r = subprocess.run([str(exe), "/nonexistent.dat", "--profile-grid", "0"], capture_output=True, text=True)
+    assert r.returncode == 2 and "block count" in r.stderr

@@ -73,6 +73,28 @@ def test_bfs_program_dat_and_snap(tmp_path):
     assert parse_block(r.stdout)["source"] == [str(g.source)]
 
 
+def test_bfs_program_frontier_profile(tmp_path):
+    """--frontier-profile prints the reference profiler's block (Dim / Siz /
+    Rng and one "L: a b c e f" line per level) before the result lines, with
+    the counts of dfq_frontier_profile on the same levels; "- Time" stays the
+    second-to-last token."""
+    g = d.gen_rmat(12, 16, seed=43)
+    g.source = int(g.pick_sources(1, seed=43)[0])
+    g.save(tmp_path / "g.dat", "dat")
+    r = subprocess.run([str(EXE), str(tmp_path / "g.dat"), "--frontier-profile", "--profile-tiles",
+                        "8,64,1024,16384", "--profile-grid", "72"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    clean = re.sub(r"\x1b\[[0-9;]*[A-Za-z]", "", r.stdout)
+    assert "Dim: 72 1024" in clean and "Siz: 8 64 1024 16384 73728" in clean and "Rng: 8 64 1024 16384 inf" in clean
+    rows = [list(map(int, m.groups())) for m in re.finditer(r"^(\d+): (\d+) (\d+) (\d+) (\d+) (\d+)$", clean, re.M)]
+    want = oracle.bfs(g.offsets, g.cols, g.source)
+    idle, _ = d.frontier_profile(g, want, (8, 64, 1024, 16384), 72 * 1024)
+    assert [row[0] for row in rows] == list(range(len(idle)))
+    assert np.array_equal(np.array([row[1:] for row in rows], np.int64), idle)
+    assert clean.index("Rng:") < clean.index("- Dist")
+    float(r.stdout.split()[-2][:-2])
+
+
 def test_bfs_program_interactive(tmp_path):
     g = d.gen_rmat(11, 8, seed=42)
     g.save(tmp_path / "g.dat", "dat")
