@@ -65,3 +65,18 @@ def test_quirks_limits_and_threads():
         d.frontier_profile(big, lv, (128, 16, 1024, 8192))   # not increasing
     with pytest.raises(d.DfqError):
         d.frontier_profile(big, lv, threads=0)
+
+
+def test_null_arguments_and_empty_graph():
+    import ctypes as C
+    L = d.lib()
+    tiles = (C.c_int32 * 4)(16, 128, 1024, 8192)
+    assert L.dfq_frontier_profile(None, None, tiles, 1024, 4, None, None) == -1
+    g = d.gen_rmat(8, 4, seed=1)
+    c = g._as_c()
+    assert L.dfq_frontier_profile(C.byref(c), None, tiles, 1024, 4, None, None) == -1
+    lv = np.full(g.n, -1, np.int32)  # nothing reached: no levels
+    idle, cnt = d.frontier_profile(g, lv)
+    assert idle.shape == (0, 5) and cnt.shape == (0, 5)
+    with pytest.raises(ValueError):
+        d.frontier_profile(g, lv[:-1])
