@@ -1,4 +1,4 @@
-"""The bfs program's host logic on the CPU: the program is built against a
+"""Host logic on the CPU.  The bfs program is built against a
 test double of the device entry points (tests/cli_double), whose BFS is a
 serial queue BFS, and its output is checked against the oracle - input
 formats, source selection, the reference's stdout block, the '$' loop,
@@ -112,3 +112,17 @@ def test_frontier_profile_lines(exe, tmp_path, tiles, grid):
     assert np.array_equal(np.array([row[1:] for row in rows], np.int64), idle)
     assert text.index("Rng:") < text.index("- Dist")
     assert r.stdout.split()[-2] == "0.125ms"
+
+
+def test_hub_first_renumbering_on_the_host(tmp_path):
+    """dfq::hub_first_csr (pools renumber wide skewed graphs with it): a C++
+    check of its properties, built against the library's host sources."""
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    out = tmp_path / "hub_first_check"
+    srcs = [CSRC / "host_graph.cpp", CSRC / "host_gen.cpp", ROOT / "tests" / "cli_double" / "hub_first_check.cpp"]
+    subprocess.run([cxx, "-O2", "-std=c++17", f"-I{ROOT / 'include'}", f"-I{CSRC}", *map(str, srcs), "-o", str(out),
+                    "-pthread"], check=True)
+    r = subprocess.run([str(out)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
