@@ -1,8 +1,10 @@
-"""Host logic on the CPU.  The bfs program is built against a
-test double of the device entry points (tests/cli_double), whose BFS is a
-serial queue BFS, and its output is checked against the oracle - input
-formats, source selection, the reference's stdout block, the '$' loop,
---json and --frontier-profile.  The GPU tests run the real program."""
+"""Host logic on the CPU.  The bfs program is built against a test double of
+the device entry points (tests/cli_double), whose BFS is a serial queue BFS,
+and its output is checked against the oracle - input formats, source
+selection, the reference's stdout block, the '$' loop, --json and
+--frontier-profile; the GPU tests run the real program.  The host hub-first
+renumbering that pools use is checked by a C++ harness built against the
+library's host sources."""
 import re
 import shutil
 import subprocess
