@@ -403,7 +403,7 @@ struct BlockShared {
     int large_pushed;               // entries this block sent to the large queue
     int large_pieces;               // pieces of those entries
     int claimed;                    // this block claimed a vertex at this level
-    int flag;                       // barrier verdict
+    int flag;                       // barrier result (1 = proceed)
     int in[5];                      // this level's input: pushed, overflow, large entries, pieces, edges
     int ovf_edges;                  // degree sum of this block's overflow pushes at this level
     int large_edges;                // degree sum of this block's large pushes at this level
