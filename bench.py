@@ -13,15 +13,20 @@ One step = 64 BFS launches, one per source, with the graph resident in HBM.
   roofline  algorithmic bytes per BFS = 4*E_R + 8*|R| + 4*N over the average
          launch time of the BFS kernel (events around each launch), against
          the measured HBM copy bandwidth.
+  parity every timed source's levels (from the untimed counter pass) against
+         the oracle, bit for bit, with the kernel's E_R; outside the timed region.
   cpu_baseline  the oracle (the reference's serial CPU BFS, restated in C) on
-         a bounded sample of the sources, 1 host core.
+         a bounded sample of the sources, 1 host core (host CPU model and
+         core count reported beside it).
   reference_gpu the reference's own kernel (design/shared-q/atomic-sa/our-sep/
          upper-bound/bfs.cu) compiled from its sources, same graph and
          sources, its "- Time" definition.
 
 --impl reference: the reference's CPU path (the oracle port; the reference's
 serial BFS is inlined in its main() and cannot be built alone) on the same
-workload, one source per step.
+workload, one source per step.  Its graph and sources come from the oracle's
+restated generator (oracle/gen.c, byte-identical to the product's), so that
+process never loads the product library; its config equals this arm's.
 Multi-GPU (torchrun): replicas only - each rank runs the full step on its own
 copy of the graph (weak scaling); value sums all ranks' edges over the
 slowest rank's time.
@@ -55,6 +60,61 @@ def peaks():
         j = json.loads(p.read_text())
         return float(j["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def host_cpu() -> dict:
+    """Model name and logical core count of this host (reported beside every CPU baseline)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not model:
+        try:
+            for line in Path("/proc/cpuinfo").read_text().splitlines():
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    import platform
+    return {"model": model or platform.processor() or platform.machine(), "nproc": os.cpu_count(),
+            "arch": platform.machine()}
+
+
+def oracle_parity(offsets, cols, sources, device_levels, device_er=None, threads=None) -> dict:
+    """Bit-exact comparison of device level arrays with the serial oracle BFS
+    (the reference's own per-run check, applied to every source), run on the
+    host's cores (ctypes releases the GIL during each oracle call).
+    device_levels(i) returns source i's level array as numpy; device_er[i], if
+    given, is the kernel's E_R for source i, checked against the oracle's."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+    oracle.lib()
+    t0 = time.perf_counter()
+    bad, er_bad, first = 0, 0, None
+    with ThreadPoolExecutor(max_workers=threads or min(16, os.cpu_count() or 1)) as ex:
+        futs = [ex.submit(oracle.bfs, offsets, cols, int(s)) for s in sources]
+        for i, f in enumerate(futs):
+            want = f.result()
+            got = device_levels(i)
+            mm = oracle.compare(want, got)["mismatches"]
+            if mm and first is None:
+                first = {"source": int(sources[i]), "mismatches": int(mm)}
+            bad += int(mm != 0)
+            if device_er is not None and int(device_er[i]) != oracle.reached_edges(offsets, want):
+                er_bad += 1
+            futs[i] = None
+    out = {"sources_checked": len(sources), "mismatches": bad, "oracle_s": round(time.perf_counter() - t0, 1)}
+    if device_er is not None:
+        out["edge_count_mismatches"] = er_bad
+    if first:
+        out["first_mismatch"] = first
+    return out
 
 
 def load_graph(scale: int = 22):
@@ -175,34 +235,56 @@ def cpu_sample(g, sources, budget_s=15.0):
     return edges, t_total, done
 
 
+def reference_workload(scale: int = 22):
+    """The headline graph and sources built through the oracle's restated
+    generator (byte-identical to the product's, tests/test_oracle_gen.py), so
+    that the reference arm never loads the product library."""
+    import oracle
+    off, cols = oracle.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed=1)
+    srcs = oracle.pick_sources(off, 64, seed=1)
+    return off, cols, srcs
+
+
 def run_reference(args, ws, rank, pg):
-    """The reference's CPU path (oracle port), one source per step."""
+    """The reference's CPU path - its serial BFS (bfs.cu:216-253), restated in
+    oracle/oracle.c because the reference inlines it in a main() built on
+    managed GPU memory - one source per step, on one host core like the
+    reference.  Graph and sources come from oracle/gen.c."""
     if rank != 0:
         return 0
     import oracle
-    g = load_graph()
-    srcs = g.pick_sources(64, seed=1)
-    oracle.lib()
+    t_gen = time.perf_counter()
+    off, cols, srcs = reference_workload(args.scale)
+    t_gen = time.perf_counter() - t_gen
+    n, e = len(off) - 1, len(cols)
     for i in range(args.warmup):
-        oracle.bfs(g.offsets, g.cols, int(srcs[i % 64]))
+        oracle.bfs(off, cols, int(srcs[i % 64]))
     edges, ts = 0, []
     for i in range(args.steps):
         s = int(srcs[i % 64])
         t0 = time.perf_counter()
-        lv = oracle.bfs(g.offsets, g.cols, s)
+        lv = oracle.bfs(off, cols, s)
         ts.append(time.perf_counter() - t0)
-        edges += oracle.reached_edges(g.offsets, lv)
+        edges += oracle.reached_edges(off, lv)
     tot = sum(ts)
     val = edges / tot / 1e9
-    line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+    metric = METRIC if args.scale == 22 else f"BFS GTEPS (RMAT-{args.scale} EF16, 64 sources one at a time)"
+    line = {"metric": metric, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
-            "config": dict(WORKLOAD, step="one source (serial CPU BFS)"), "impl": "reference",
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
+            "config": workload_config(n, e, ws), "impl": "reference",
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": f"{args.steps} sources of the 64, one serial BFS each"},
-            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": f"{args.steps} of the 64 sources (one per step), serial oracle BFS",
+                             "host": host_cpu()},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "step": "one source (serial CPU BFS)", "gen_s": round(t_gen, 1)}
     print(json.dumps(line))
     return 0
+
+
+def workload_config(n: int, e: int, ws: int) -> dict:
+    """The headline workload's config, identical in both arms."""
+    return dict(WORKLOAD, n=int(n), e=int(e), parallelism=f"replicas x{ws}")
 
 
 def pool256_graphs(seed: int = 1, count: int = 256):
@@ -426,7 +508,7 @@ def workload_graph(name: str, scale: int):
     import dfqbfs as d
     if name == "rmat22":
         g = load_graph(scale)
-        return g, g.pick_sources(64, seed=1), dict(WORKLOAD, n=g.n, e=g.e)
+        return g, g.pick_sources(64, seed=1), dict(WORKLOAD, n=int(g.n), e=int(g.e))
     if name == "grid4096":
         g, orig = d.gen_grid(4096, 0.01, seed=1)
         srcs = np.array(grid_sources(orig, 4096), np.int32)
@@ -439,19 +521,22 @@ def workload_graph(name: str, scale: int):
     raise SystemExit(f"unknown workload {name}")
 
 
-def measure_device(dg, srcs, n, steps, warmup, torch, with_clocks=None):
+def measure_device(dg, srcs, n, steps, warmup, torch, with_clocks=None, keep_levels=False):
     """Device-resident timing of `steps` passes over srcs (one launch per
     source); returns total ms (events on the graph's stream), per-launch ms,
-    per-source E_R / |R| / levels."""
+    per-source E_R / |R| / levels, and with keep_levels each source's level
+    array from the untimed pass (host copies, for the oracle check)."""
     stream = torch.cuda.ExternalStream(dg.stream)
     levels = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)]
-    er, rr, lvls = [], [], []
+    er, rr, lvls, host_levels = [], [], [], []
     for s in srcs:  # untimed pass: E_R and |R| from the kernel's own counters
         dg.launch(int(s), levels[0])
         st = dg.last_stats()
         er.append(st.edges)
         rr.append(st.reached)
         lvls.append(st.levels)
+        if keep_levels:
+            host_levels.append(levels[0].cpu().numpy())
 
     def step(evs=None):
         for i, s in enumerate(srcs):
@@ -480,7 +565,8 @@ def measure_device(dg, srcs, n, steps, warmup, torch, with_clocks=None):
     dg.sync()
     launch_ms = np.array([[a.elapsed_time(b) for (a, b) in row] for row in evs])
     return {"ms_total": t0.elapsed_time(t1), "launch_ms": launch_ms, "er": np.array(er, np.int64),
-            "rr": np.array(rr, np.int64), "levels": np.array(lvls), "levels_buf": levels}
+            "rr": np.array(rr, np.int64), "levels": np.array(lvls), "levels_buf": levels,
+            "host_levels": host_levels}
 
 
 def main():
@@ -501,6 +587,7 @@ def main():
                     help="R-MAT scale (22 is the benchmark; smaller scales are for profiler captures)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer end-to-end leg")
     ap.add_argument("--no-do", action="store_true", help="skip the direction-optimising line (reported separately)")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of every timed source")
     args = ap.parse_args()
     ws, rank, local, pg = dist_setup(args.gpus)
     if args.impl == "reference":
@@ -523,7 +610,8 @@ def main():
     n = g.n
     barrier(pg)
     ck = Clocks(local)
-    m = measure_device(dg, srcs, n, args.steps, args.warmup, torch, with_clocks=ck)
+    m = measure_device(dg, srcs, n, args.steps, args.warmup, torch, with_clocks=ck,
+                       keep_levels=(rank == 0 and not args.no_parity))
     barrier(pg)
     er, rr = m["er"], m["rr"]
     step_edges = int(er.sum())
@@ -569,8 +657,8 @@ def main():
     out = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
-           "config": dict(cfg, sources=len(srcs), parallelism=f"replicas x{ws}", opts=dg.opts().as_dict(),
-                          edges_per_step=step_edges, gen_s=round(t_gen, 2)),
+           "config": dict(cfg, sources=len(srcs), parallelism=f"replicas x{ws}"),
+           "kernel_opts": dg.opts().as_dict(), "edges_per_step": step_edges, "gen_s": round(t_gen, 2),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                         "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                         "kernel": "dfq_bfs_kernel", "bytes_alg_per_launch": bytes_per_launch,
@@ -587,12 +675,17 @@ def main():
         out["graph500_gteps"] = value / 2
     if args.workload == "rmat22" and not args.no_do:
         out["direction_optimizing"] = direction_optimizing(g, srcs, er, levels, args, torch, d, pg)
+    if rank == 0 and not args.no_parity:
+        # every timed source's levels (from the untimed pass) against the oracle
+        out["parity"] = oracle_parity(g.offsets, g.cols, srcs, lambda i: m["host_levels"][i], device_er=er)
+        m["host_levels"].clear()
     if rank == 0 and not args.no_cpu:
         import oracle
         oracle.lib()
         edges, tcpu, nsrc = cpu_sample(g, srcs, budget_s=15.0)
         out["cpu_baseline"] = {"value": edges / tcpu / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
-                               "sample": f"{nsrc} of the {len(srcs)} sources, serial oracle BFS, {tcpu:.1f} s"}
+                               "sample": f"{nsrc} of the {len(srcs)} sources, serial oracle BFS, {tcpu:.1f} s",
+                               "host": host_cpu()}
     if rank == 0 and not args.no_ref_gpu:
         import oracle
         k = 16 if args.workload == "rmat22" else 2
@@ -630,16 +723,19 @@ def direction_optimizing(g, srcs, er, td_levels, args, torch, d, pg):
 
 
 def secondary_grid(torch, d, args):
-    """The 4096^2 grid (high diameter): GTEPS and microseconds per level on 4 of its
-    16 sources (2 corners, 2 interior), next to the reference kernel."""
+    """The 4096^2 grid (high diameter): GTEPS and microseconds per level over its
+    16 sources (4 corners, 12 interior), every source checked against the
+    oracle, next to the reference kernel on one of them."""
     g, srcs, cfg = workload_graph("grid4096", 22)
-    srcs = np.array([srcs[0], srcs[3], srcs[4], srcs[5]], np.int32)
     with d.Graph(g) as dg:
-        m = measure_device(dg, srcs, g.n, 1, 1, torch)
+        m = measure_device(dg, srcs, g.n, 1, 1, torch, keep_levels=not args.no_parity)
     ms = m["launch_ms"][0]
     res = {"workload": cfg["workload"], "sources": srcs.tolist(), "gteps": float(m["er"].sum() / (ms.sum() * 1e-3) / 1e9),
            "ms_median": float(np.median(ms)), "levels_median": float(np.median(m["levels"])),
            "us_per_level": float(np.median(ms * 1e3 / np.maximum(m["levels"], 1)))}
+    if not args.no_parity:
+        res["parity"] = oracle_parity(g.offsets, g.cols, srcs, lambda i: m["host_levels"][i], device_er=m["er"])
+        m["host_levels"].clear()
     if not args.no_ref_gpu:
         res["reference_gpu"] = reference_gpu(g, srcs[:1], max_sources=1)
     return res

@@ -9,6 +9,10 @@
 #include <thread>
 #include <vector>
 
+namespace dfqk {
+struct Control;
+}
+
 namespace dfq {
 
 // Record a message for dfq_last_error() on this host thread and return `code`.
@@ -57,11 +61,15 @@ int build_csr(const std::vector<EdgeSpan>& spans, int32_t n, int32_t flags, dfq_
 int hub_first_csr(const dfq_csr& in, int mode, dfq_csr* out, std::vector<int32_t>* rank,
                   std::vector<int32_t>* order);
 
-// Set kernel fn's dynamic shared-memory limit to what the next launch needs.
-// The limit is a property of the function, shared by every graph, pool and
-// entry point launching it, so it is set right before each launch (never
-// cached per caller: another caller may have set a smaller value since).
+// Make sure kernel fn's dynamic shared-memory limit on the current device is
+// at least what the next launch needs.  The limit is a property of the
+// function, shared by every graph, pool and entry point launching it, so it
+// only ever rises (under a lock): no caller can lower it under another's launch.
 int allow_dyn_smem(const void* fn, int smem_needed);
+
+// DFQ_OK for a launch whose control block reports no device error, else the
+// matching status (DFQ_ETIMEOUT, DFQ_EDEVICE) with its message recorded.
+int device_status(const dfqk::Control& c);
 
 // The single-source kernel dfqk::dfq_bfs_kernel<block_threads, par>, compiled
 // once (in dfq_api.cu) and launched through this handle by every entry point

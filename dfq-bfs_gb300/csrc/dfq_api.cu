@@ -409,7 +409,7 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
     const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
     const int hot_words = hot_words_for(o, g->n);
     const int smem = lay.bytes + 4 * hot_words;
-    // the limit is shared with every other caller of this kernel: set it each time
+    // the limit is shared with every other caller of this kernel
     if (int rc = allow_dyn_smem((const void*)k, smem)) return rc;
     if ((const void*)k != g->cfg_kernel || smem != g->cfg_smem || o.blocks_per_sm != g->cfg_bps) {
         int per_sm = 0;
@@ -516,10 +516,29 @@ struct DeviceGuard {
 
 namespace dfq {
 int allow_dyn_smem(const void* fn, int smem_needed) {
+    // The limit only ever rises (per kernel and device, under one lock): a
+    // limit above what a launch uses costs nothing, while lowering it could
+    // fail another host thread's launch that set a larger value just before.
+    static std::mutex mu;
+    static std::vector<std::pair<std::pair<const void*, int>, int>> set_to;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto& kv : set_to)
+        if (kv.first.first == fn && kv.first.second == dev) {
+            if (kv.second >= smem_needed) return DFQ_OK;
+            cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_needed);
+            if (err != cudaSuccess) return fail(DFQ_ECUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(err));
+            kv.second = smem_needed;
+            return DFQ_OK;
+        }
     cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_needed);
     if (err != cudaSuccess) return fail(DFQ_ECUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(err));
+    set_to.push_back({{fn, dev}, smem_needed});
     return DFQ_OK;
 }
+
+int device_status(const dfqk::Control& c) { return map_device_status(c); }
 
 const void* single_source_kernel(int block_threads, bool par) {
     return (const void*)pick_kernel(block_threads, par);

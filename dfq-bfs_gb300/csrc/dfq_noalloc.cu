@@ -24,6 +24,12 @@
 // with cudaGetSymbolAddress (host code cannot use the array's name as a device
 // pointer) and caches it with the kernel's launch shape; make that first call
 // before any stream capture.
+//
+// Cost: every call first checks the caller's CSR on the device (one pass over
+// the n + 1 offsets and the e columns, about 4 bytes per edge) and waits for
+// that check before the traversal, whose algorithmic traffic is also about 4
+// bytes per edge, so a call moves up to twice the bytes of dfq_bfs on a graph
+// handle (which checks its CSR once, at creation).
 #include "common.hpp"
 #include "dfq_kernel.cuh"
 
@@ -209,10 +215,5 @@ extern "C" int dfq_bfs_noalloc(const int32_t* offsets, const int32_t* cols, int3
         stats->overflow = (int64_t)host_ctl.stats.overflow;
         stats->large = (int64_t)host_ctl.stats.large;
     }
-    switch (host_ctl.status) {
-        case dfqk::kErrNone: return DFQ_OK;
-        case dfqk::kErrBarrierTimeout:
-        case dfqk::kErrTmaTimeout: return fail(DFQ_ETIMEOUT, "dfq_bfs_noalloc: a bounded device wait timed out");
-        default: return fail(DFQ_EDEVICE, "dfq_bfs_noalloc: device status %d", host_ctl.status);
-    }
+    return device_status(host_ctl);
 }

@@ -412,7 +412,9 @@ int dfq_server_destroy(dfq_server* s);
  * 24 * n + e / 5 bytes of scratch (about 1.2 million vertices at average
  * degree 16); larger graphs are rejected with DFQ_ENOMEM and a message naming
  * the bytes needed.  cols must be 16-byte aligned.  The CSR is checked on the
- * device first (DFQ_EFORMAT if malformed).
+ * device first (DFQ_EFORMAT if malformed); that check reads every offset and
+ * column once more per call, so a call moves up to twice the bytes of
+ * dfq_bfs on a graph handle, which checks its CSR once at creation.
  *
  * Runs on `stream` (null = the legacy default stream) with the default
  * dfq_opts and returns after the BFS has finished; stats (nullable) gets the

@@ -7,6 +7,9 @@ it.  Contents:
   * oracle.c (built to oracle/build/liboracle.so): the reference's serial CPU
     BFS (design/shared-q/atomic-sa/our-sep/upper-bound/bfs.cu:216-253), its
     validation rule (:290-296), BFS-tree validation and E_R.
+  * gen.c (same library): the seeded R-MAT generator and source picker,
+    restated so the reference-side benchmark arm builds its workload without
+    loading the product library (checked byte for byte against it).
   * py_bfs / py_compare: the same algorithm in pure Python, for tiny graphs,
     used to cross-check the C restatement.
   * refgpu: runs the reference's own kernel (compiled from the reference
@@ -43,6 +46,14 @@ def lib() -> C.CDLL:
         L.oracle_reached_edges.restype = C.c_int64
         L.oracle_level_histogram.argtypes = [C.c_int32, P, C.POINTER(C.c_int64), C.c_int32]
         L.oracle_level_histogram.restype = C.c_int32
+        PP = C.POINTER(P)
+        L.gen_rmat_undirected.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                          C.c_int, PP, PP]
+        L.gen_rmat_undirected.restype = C.c_int64
+        L.gen_pick_sources.argtypes = [C.c_int32, P, C.c_int32, C.c_uint64, P]
+        L.gen_pick_sources.restype = C.c_int
+        L.gen_free.argtypes = [C.c_void_p]
+        L.gen_free.restype = None
         _lib = L
     return _lib
 
@@ -85,6 +96,35 @@ def validate_tree(offsets, cols, src: int, levels, parents) -> int:
 def reached_edges(offsets, levels) -> int:
     off = _i32(offsets)
     return int(lib().oracle_reached_edges(len(off) - 1, _p(off), _p(_i32(levels))))
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1, threads: int | None = None):
+    """(offsets, cols) of the symmetrised, de-duplicated, self-loop-free R-MAT
+    graph the product's generator makes with the same arguments."""
+    import os
+    P = C.POINTER(C.c_int32)
+    off_p, col_p = P(), P()
+    t = threads if threads is not None else (os.cpu_count() or 1)
+    e = lib().gen_rmat_undirected(scale, edge_factor, a, b, c, seed, t, C.byref(off_p), C.byref(col_p))
+    if e < 0:
+        raise ValueError("gen_rmat_undirected failed")
+    n = 1 << scale
+    off = np.ctypeslib.as_array(off_p, shape=(n + 1,)).copy()
+    cols = np.ctypeslib.as_array(col_p, shape=(max(int(e), 1),))[: int(e)].copy()
+    lib().gen_free(C.cast(off_p, C.c_void_p))
+    lib().gen_free(C.cast(col_p, C.c_void_p))
+    return off, cols
+
+
+def pick_sources(offsets, k: int, seed: int) -> np.ndarray:
+    """k seeded sources among the vertices of out-degree > 0 (the product's
+    picker, restated)."""
+    off = _i32(offsets)
+    out = np.zeros(k, np.int32)
+    if lib().gen_pick_sources(len(off) - 1, _p(off), k, seed, _p(out) if k else None) != 0:
+        raise ValueError("gen_pick_sources: no vertex with out-degree > 0")
+    return out
 
 
 # ------------------------------------------------------------ pure Python

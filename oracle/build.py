@@ -1,10 +1,10 @@
 """Build recipe for the oracle (test infrastructure only).
 
-  build_oracle()  gcc oracle.c -> oracle/build/liboracle.so   (any machine)
+  build_oracle()  gcc oracle.c gen.c -> oracle/build/liboracle.so   (any machine)
   build_refgpu()  g++ refgpu.cpp -> oracle/build/librefgpu.so  (loader of the
                   reference's kernel; driver API, any machine with CUDA)
   build_ref()     compiles the REFERENCE's own kernel sources, where they lie
-                  under /root/reference, into device code only
+                  under /root/reference (or $DFQ_REFERENCE), into device code only
                   (oracle/_ref/*.cubin, sm_103a).  Device code carries no host
                   architecture, so a cubin built here runs from the loader
                   built on the GPU machine.  The reference sources need one
@@ -22,7 +22,9 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "build"
 REF_OUT = HERE / "_ref"
-REFERENCE = Path("/root/reference")
+# where the reference project lies (only the recipe that compiles its kernels
+# reads it); DFQ_REFERENCE overrides the default location
+REFERENCE = Path(os.environ.get("DFQ_REFERENCE", "/root/reference"))
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 CUDA_HOME = str(Path(NVCC).resolve().parent.parent)
 
@@ -51,8 +53,9 @@ def _run(cmd) -> None:
 def build_oracle() -> Path:
     OUT.mkdir(exist_ok=True)
     lib = OUT / "liboracle.so"
-    if _stale(lib, [HERE / "oracle.c"]):
-        _run(["gcc", "-O2", "-std=c99", "-fPIC", "-shared", str(HERE / "oracle.c"), "-o", str(lib)])
+    srcs = [HERE / "oracle.c", HERE / "gen.c"]
+    if _stale(lib, srcs):
+        _run(["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", *map(str, srcs), "-o", str(lib), "-lpthread", "-lm"])
     return lib
 
 

@@ -93,27 +93,33 @@ int64_t oracle_compare(int32_t n, const int32_t* want, const int32_t* got, int64
  *   levels[v] == -1  <=>  parents[v] == -1;
  *   otherwise p = parents[v] is in range, levels[p] == levels[v] - 1, and the
  *   edge p -> v exists in the CSR.
+ * The edge check is one pass over the CSR (every edge u -> v with
+ * parents[v] == u marks v), so the cost is O(n + e) whatever the degrees.
  * Returns 0 if valid, else 1 + the first offending vertex (so a caller can
- * report it). */
+ * report it), or -1 if the scratch allocation fails. */
 int64_t oracle_validate_tree(int32_t n, const int32_t* offsets, const int32_t* cols, int32_t src,
                              const int32_t* levels, const int32_t* parents) {
     if (src < 0 || src >= n) return 1;
     if (parents[src] != src || levels[src] != 0) return 1 + (int64_t)src;
-    for (int32_t v = 0; v < n; ++v) {
+    unsigned char* has_edge = (unsigned char*)calloc((size_t)n, 1);
+    if (!has_edge) return -1;
+    for (int32_t u = 0; u < n; ++u)
+        for (int32_t j = offsets[u]; j < offsets[u + 1]; ++j) {
+            const int32_t v = cols[j];
+            if (parents[v] == u) has_edge[v] = 1;
+        }
+    int64_t bad = 0;
+    for (int32_t v = 0; v < n && !bad; ++v) {
         if (v == src) continue;
         const int32_t p = parents[v];
         if (levels[v] < 0) {
-            if (p != -1) return 1 + (int64_t)v;
+            if (p != -1) bad = 1 + (int64_t)v;
             continue;
         }
-        if (p < 0 || p >= n) return 1 + (int64_t)v;
-        if (levels[p] != levels[v] - 1) return 1 + (int64_t)v;
-        int found = 0;
-        for (int32_t j = offsets[p]; j < offsets[p + 1]; ++j)
-            if (cols[j] == v) { found = 1; break; }
-        if (!found) return 1 + (int64_t)v;
+        if (p < 0 || p >= n || levels[p] != levels[v] - 1 || !has_edge[v]) bad = 1 + (int64_t)v;
     }
-    return 0;
+    free(has_edge);
+    return bad;
 }
 
 /* E_R: sum of out-degrees over vertices with levels >= 0. */

@@ -59,13 +59,17 @@ def test_gloo_replica_reductions():
 
 def test_reference_arm_rank0_only(tmp_path):
     """bench.py --impl reference under two ranks: rank 0 prints the line,
-    rank 1 exits 0 without work (tiny workload via a cached small graph)."""
+    rank 1 exits 0 without work (a small R-MAT scale keeps it quick).  The
+    arm builds its workload through the oracle alone: the product library is
+    never loaded in that process."""
     pytest.importorskip("torch.distributed")
     code = (f"import sys; sys.path[:0]=[{str(ROOT)!r}+'/dfq-bfs_gb300', {str(ROOT)!r}]; "
-            "import bench, dfqbfs as d; "
-            "bench.load_graph = lambda scale=22: d.gen_rmat(10, 8, seed=1); "
-            "sys.argv=['bench.py','--impl','reference','--gpus','2','--steps','2','--warmup','1']; "
-            "sys.exit(bench.main())")
+            "import bench; "
+            "sys.argv=['bench.py','--impl','reference','--gpus','2','--steps','2','--warmup','1','--scale','10']; "
+            "rc = bench.main(); "
+            "assert 'dfqbfs' not in sys.modules; "
+            "assert not [l for l in open('/proc/self/maps') if 'libdfq' in l]; "
+            "sys.exit(rc)")
     procs, outs = run_ranks(code, free_port())
     for p, o in zip(procs, outs):
         assert p.returncode == 0, o[1]

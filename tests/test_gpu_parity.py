@@ -409,16 +409,45 @@ def test_autotune_keeps_parity():
             run_and_check(g, int(s), graph=dg)
 
 
-@pytest.mark.parametrize("cfg", ["rmat22", "grid4096"])
-def test_full_size_configs(cfg):
-    """Full-size R-MAT scale 22 and the 4096^2 grid with 1% of edges deleted: bit-exact
-    against the oracle for a few sources."""
-    if cfg == "rmat22":
-        g = d.gen_rmat(22, 16, seed=1)
-        srcs = g.pick_sources(64, seed=1)[:2]
-    else:
-        g, orig = d.gen_grid(4096, 0.01, seed=1)
-        srcs = [0, g.n - 1]
-    with d.Graph(g) as dg:
-        for s in srcs:
-            run_and_check(g, int(s), graph=dg, parents=(cfg == "rmat22"))
+def _check_all_sources(g, srcs, parents):
+    """Every source through dfq_bfs, bit-exact against the oracle (run on the
+    host's cores in threads: ctypes releases the GIL), parents validated as a
+    BFS tree, kernel E_R and reached count equal to the oracle's."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    oracle.lib()
+    workers = min(16, os.cpu_count() or 1)
+    with d.Graph(g) as dg, ThreadPoolExecutor(max_workers=workers) as ex:
+        wants = [ex.submit(oracle.bfs, g.offsets, g.cols, int(s)) for s in srcs]
+        checks = []
+        for i, s in enumerate(srcs):
+            lv, pa, st = dg.bfs(int(s), parents=parents)
+
+            def check(i=i, s=int(s), lv=lv, pa=pa, st=st):
+                want = wants[i].result()
+                cmp = oracle.compare(want, lv)
+                tree = oracle.validate_tree(g.offsets, g.cols, s, lv, pa) if parents else 0
+                er = oracle.reached_edges(g.offsets, want)
+                wants[i] = None
+                return s, cmp["mismatches"], tree, st.edges == er, st.reached == int((want >= 0).sum())
+            checks.append(ex.submit(check))
+        bad = [c.result() for c in checks]
+    bad = [b for b in bad if b[1] or b[2] or not b[3] or not b[4]]
+    assert not bad, f"sources failing (source, level mismatches, tree, E_R ok, reached ok): {bad[:4]}"
+
+
+def test_full_size_rmat22_every_source():
+    """RMAT scale 22, edge factor 16: all 64 benchmark sources (pick_sources(64,
+    seed=1)), levels bit-exact, parents a BFS tree."""
+    g = d.gen_rmat(22, 16, seed=1)
+    _check_all_sources(g, g.pick_sources(64, seed=1), parents=True)
+
+
+def test_full_size_grid4096_every_source():
+    """The 4096^2 grid with 1% of edges deleted (largest component): all 16
+    benchmark sources (4 corners, 12 seeded interior vertices)."""
+    import bench
+    g, orig = d.gen_grid(4096, 0.01, seed=1)
+    srcs = bench.grid_sources(orig, 4096)
+    assert len(srcs) == 16
+    _check_all_sources(g, srcs, parents=False)

@@ -45,8 +45,32 @@ def test_noalloc_matches_dfq_bfs_two_calls(torch):
             st = d.bfs_noalloc(off, cols, g.n, g.e, src, lv, pa)
             got = lv.cpu().numpy()
             assert np.array_equal(got, want), f"call {call}: levels differ from dfq_bfs"
+            assert oracle.compare(oracle.bfs(g.offsets, g.cols, src), got)["mismatches"] == 0
             assert oracle.validate_tree(g.offsets, g.cols, src, got, pa.cpu().numpy()) == 0
             assert st.edges == wst.edges and st.reached == wst.reached and st.depth == wst.depth
+
+
+def test_noalloc_allocates_no_device_memory(torch):
+    """What the entry point exists for: after a first call (which sets up the
+    device), further calls change neither the device's free memory nor what
+    torch's caching allocator holds."""
+    g = d.gen_rmat(14, 16, seed=80)
+    off, cols = device_csr(torch, g)
+    lv = torch.empty(g.n, dtype=torch.int32, device="cuda")
+    pa = torch.empty(g.n, dtype=torch.int32, device="cuda")
+    srcs = [int(s) for s in g.pick_sources(4, seed=80)]
+    d.bfs_noalloc(off, cols, g.n, g.e, srcs[0], lv, pa)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    reserved0 = torch.cuda.memory_reserved()
+    for s in srcs:
+        d.bfs_noalloc(off, cols, g.n, g.e, s, lv, pa)
+        d.bfs_noalloc(off, cols, g.n, g.e, s, lv)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, f"device free memory changed by {free0 - free1} bytes"
+    assert torch.cuda.memory_reserved() == reserved0
+    assert oracle.compare(oracle.bfs(g.offsets, g.cols, srcs[-1]), lv.cpu().numpy())["mismatches"] == 0
 
 
 def test_noalloc_same_source_twice_without_parents(torch):
@@ -58,6 +82,7 @@ def test_noalloc_same_source_twice_without_parents(torch):
         lv = torch.empty(g.n, dtype=torch.int32, device="cuda")
         d.bfs_noalloc(off, cols, g.n, g.e, 0, lv)
         assert np.array_equal(lv.cpu().numpy(), want)
+        assert oracle.compare(oracle.bfs(g.offsets, g.cols, 0), lv.cpu().numpy())["mismatches"] == 0
 
 
 def test_noalloc_rejects_what_it_cannot_hold(torch):
