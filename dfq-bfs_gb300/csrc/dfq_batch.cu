@@ -45,6 +45,7 @@ struct BatchParams {
     int medium_min, large_min, piece_edges, local_cap, local_budget, probe_first, use_tma;
     long long timeout_ns;
     int hot_words;  // hot-vertex cache words this launch reserves (0: none)
+    int cold;       // 1: the launch's layout has cold rings (whenever hot_words > 0)
     int reserve;    // blocks that run narrow queries during the wide phase
 };
 
@@ -78,6 +79,7 @@ __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, i
     sp.use_tma = bp.use_tma;
     sp.timeout_ns = bp.timeout_ns;
     sp.hot_words = hot_words_of(bp.hot_words, g.n);
+    sp.cold = bp.cold;
     remap_params(sp, g, ws);  // renumbered graphs are wide: only the grid's workspace has room
 }
 
@@ -252,6 +254,8 @@ int dfq_pool_create(const dfq_csr* graphs, int32_t ngraphs, const dfq_opts* opts
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, p->device) != cudaSuccess) { pool_release(p); return fail(DFQ_ECUDA, "no CUDA device"); }
     p->sms = prop.multiProcessorCount;
+    p->sm_smem = (int)prop.sharedMemPerMultiprocessor;
+    p->block_smem = (int)prop.sharedMemPerBlockOptin;
     int64_t tot_n = 0, tot_e = 0;
     std::vector<int64_t> off_base(ngraphs), col_base(ngraphs);
     for (int i = 0; i < ngraphs; ++i) {
@@ -372,8 +376,8 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     const dfq_opts& o = p->opts;
     const void* fn = single_source_kernel(o.block_threads, par);
     if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
-    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
-    const int hot = hot_limit_words(o.hot_cache) > 0 ? hot_words_of(hot_limit_words(o.hot_cache), p->n[graph]) : 0;
+    const int hot = hot_words_of(pool_hot_words(p, par), p->n[graph]);
+    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par, hot > 0);
     const int smem = lay.bytes + 4 * hot;
     int grid = 0;
     if ((rc = grid_for(p, fn, o.block_threads, smem, &grid))) return rc;
@@ -406,6 +410,7 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     prm.use_tma = o.use_tma;
     prm.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     prm.hot_words = hot;
+    prm.cold = hot > 0;
     remap_params(prm, p->h_graphs[graph], w);
     cudaEventRecord(p->ev0, p->stream);
     cudaMemsetAsync(p->d_ctl1, 0, sizeof(Control), p->stream);
@@ -446,12 +451,10 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     const dfq_opts& o = p->opts;
     const void* fn = pick_batch(o.block_threads, par);
     if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
-    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
     // one cache size per pool (the largest graph's), so a captured launch
-    // stays valid for any batch of the same shape
-    int hot = 0;
-    if (hot_limit_words(o.hot_cache) > 0)  // the cache only on request
-        for (int i = 0; i < p->ngraphs; ++i) hot = std::max(hot, hot_words_of(hot_limit_words(o.hot_cache), p->n[i]));
+    // stays valid for any batch of the same shape; the cache only on request
+    const int hot = pool_hot_words(p, par);
+    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par, hot > 0);
     const int smem = lay.bytes + 4 * hot;
     int grid = 0, rc;
     if ((rc = grid_for(p, fn, o.block_threads, smem, &grid))) return rc;
@@ -500,6 +503,7 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     bp.use_tma = o.use_tma;
     bp.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     bp.hot_words = hot;
+    bp.cold = hot > 0;
     // a sixth of the grid starts the narrow queries while the rest runs the
     // wide ones (when there are both; measured on the 256-graph pool: 1/16
     // 16.1k, 1/8 17.0-18.0k, 1/6 18.1k, 1/4 17.1k queries/s)

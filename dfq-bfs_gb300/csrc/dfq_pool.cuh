@@ -97,6 +97,8 @@ struct dfq_pool {
     using PoolGraph = dfqk::PoolGraph;
     int device = 0;
     int sms = 0;
+    int sm_smem = 0;     // shared memory per SM (bytes)
+    int block_smem = 0;  // opt-in shared memory per block (bytes)
     dfq_opts opts{};
     int32_t ngraphs = 0;
     std::vector<int32_t> n;
@@ -216,6 +218,17 @@ inline int ensure_wide(dfq_pool* p, bool par) {
     p->wide_lay = ws_layout(nmax, emax, kMinLarge, kMinPiece, par, remap);
     p->wide_par = par;
     return dmalloc(&p->wide_mem, p->wide_lay.total);
+}
+
+// Hot-vertex cache words a launch over the pool reserves per block (the
+// largest graph's, cut to what fits; 0 unless the options ask for a cache).
+inline int pool_hot_words(const dfq_pool* p, bool par) {
+    const dfq_opts& o = p->opts;
+    long long nmax = 1;
+    for (int i = 0; i < p->ngraphs; ++i) nmax = std::max<long long>(nmax, p->n[i]);
+    const int blocks = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, 1024 / o.block_threads) : 1024 / o.block_threads;
+    return launch_hot_words(o.hot_cache, nmax, o.block_threads, o.local_queue_cap, o.piece_edges, par, blocks,
+                            p->sm_smem, p->block_smem);
 }
 
 inline int grid_for(dfq_pool* p, const void* fn, int B, int smem, int* grid) {

@@ -89,7 +89,7 @@ def test_batch_with_hot_cache(torch, flags):
     block), with parents: same levels, valid trees."""
     graphs = mixed_graphs()
     o = opts_small_wide()
-    o.hot_cache = 1
+    o.hot_cache = 64  # as large as fits beside the layout (with cold rings)
     with d.Pool(graphs, o) as pool:
         qs, meta = make_queries(torch, graphs, 2, seed=5, parents=True)
         res, _ = pool.batch(qs, flags)

@@ -180,16 +180,41 @@ def test_level_profile_matches_oracle(kind):
     assert np.all(np.diff(ns) >= 0)
 
 
-@pytest.mark.parametrize("order,hot", [(1, 0), (2, 0), (2, -1), (1, 1), (2, 1)])
-def test_vertex_order_and_hot_cache(order, hot):
-    """Hub-first relabelling and the shared hot-vertex cache change only how
-    the kernel works: levels, parents (in input ids) and E_R stay exact, on
-    the whole grid and in a small graph that the cache covers entirely."""
+@pytest.mark.parametrize("order,hot,block", [(1, 0, 512), (2, 0, 512), (2, -1, 512), (1, 64, 512), (2, 64, 512),
+                                             (2, 8, 512), (2, 64, 1024), (1, 64, 256)])
+def test_vertex_order_and_hot_cache(order, hot, block):
+    """Hub-first relabelling and the shared hot-vertex cache (with the cold
+    rings that batch the probes it cannot settle) change only how the kernel
+    works: levels, parents (in input ids) and E_R stay exact, on the whole
+    grid and in a small graph that the cache covers entirely."""
     for g, srcs in [(d.gen_rmat(16, 16, seed=21), None), (d.gen_zipf_geometric(50000, 4.7, 2.1, seed=21), [0, 7])]:
         srcs = srcs or [int(x) for x in g.pick_sources(3, seed=21)]
-        with d.Graph(g, opts=opts(vertex_order=order, hot_cache=hot)) as dg:
+        with d.Graph(g, opts=opts(vertex_order=order, hot_cache=hot, block_threads=block)) as dg:
             for s in srcs:
                 run_and_check(g, int(s), graph=dg)
+                run_and_check(g, int(s), graph=dg, parents=False)
+
+
+@pytest.mark.parametrize("block", [256, 512, 1024])
+@pytest.mark.parametrize("tma", [0, 1])
+def test_hot_cache_cold_rings_bin_boundaries(block, tma):
+    """The cold-ring probe path on a hub graph whose degrees sit on every bin
+    boundary (small gather, medium warp lists, large pieces), hub-first ids
+    forced so the cache holds the hubs: bit-exact levels, valid parents."""
+    rng = np.random.default_rng(31)
+    n = 1 << 15
+    src, dst = [], []
+    for h, k in enumerate([1, 31, 32, 33, 63, 64, 65, 255, 256, 257, 511, 1023, 1024, 4095, 4096, 16385]):
+        src += [h] * k
+        dst += rng.choice(n, size=k, replace=False).tolist()
+    m = 12 * n
+    src += rng.integers(0, n, m).tolist()
+    dst += (rng.zipf(2.0, m) % n).tolist()
+    g = d.from_edges(src, dst, n, d.CSR_SYMMETRIZE | d.CSR_DEDUP)
+    with d.Graph(g, opts=opts(hot_cache=64, vertex_order=2, block_threads=block, use_tma=tma)) as dg:
+        for s in [0, 7, 15, int(rng.integers(0, n))]:
+            run_and_check(g, s, graph=dg)
+            run_and_check(g, s, graph=dg, parents=False)
 
 
 def test_hub_first_auto_and_device_input():
@@ -397,6 +422,22 @@ def test_single_vertex_and_empty_graph():
     run_and_check(g, 0)
     g = d.from_edges([], [], 50)
     run_and_check(g, 13)
+
+
+@pytest.mark.parametrize("kw", [{"l2_persist": 1}, {"blocks_per_sm": 1}, {"blocks_per_sm": 2},
+                                {"blocks_per_sm": 1, "block_threads": 1024, "hot_cache": 64},
+                                {"l2_persist": 1, "hot_cache": 64, "vertex_order": 2}])
+def test_autotuner_axes_keep_parity(kw):
+    """Every option the autotuner can pick runs bit-exact: the L2-persisting
+    bitmap window, capped blocks per SM, and the hot-vertex cache with its
+    cold rings, on a skewed graph (hub-first ids) and a grid."""
+    rm = d.gen_rmat(17, 16, seed=41)
+    grid, _ = d.gen_grid(256, 0.02, seed=41)
+    for g, srcs in [(rm, [int(x) for x in rm.pick_sources(3, seed=41)]), (grid, [0, grid.n // 2])]:
+        with d.Graph(g, opts=opts(**kw)) as dg:
+            for s in srcs:
+                run_and_check(g, s, graph=dg)
+                run_and_check(g, s, graph=dg, parents=False)
 
 
 def test_autotune_keeps_parity():
