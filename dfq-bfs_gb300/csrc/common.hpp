@@ -71,6 +71,10 @@ int allow_dyn_smem(const void* fn, int smem_needed);
 // matching status (DFQ_ETIMEOUT, DFQ_EDEVICE) with its message recorded.
 int device_status(const dfqk::Control& c);
 
+// DFQ_OK if every field of o is in range and its shared-memory layout fits a
+// block, else DFQ_EINVAL with the reason recorded.
+int check_opts(const dfq_opts& o);
+
 // The single-source kernel dfqk::dfq_bfs_kernel<block_threads, par>, compiled
 // once (in dfq_api.cu) and launched through this handle by every entry point
 // that runs one BFS on a whole cooperative grid; null for an unsupported size.

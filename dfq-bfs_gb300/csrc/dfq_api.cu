@@ -29,8 +29,6 @@ using namespace dfq;
 struct dfq_graph {
     int device = 0;
     int sms = 0;
-    int sm_smem = 0;     // shared memory per SM (bytes)
-    int block_smem = 0;  // opt-in shared memory per block (bytes)
     int32_t n = 0;
     int64_t e = 0;
     dfq_opts opts{};
@@ -100,15 +98,13 @@ int validate_opts(const dfq_opts& o) {
     if (o.local_edge_budget < 0) return fail(DFQ_EINVAL, "local_edge_budget must be >= 0");
     if (o.timeout_ms < 1) return fail(DFQ_EINVAL, "timeout_ms must be >= 1");
     if (o.probe_first < 0 || o.probe_first > 2) return fail(DFQ_EINVAL, "probe_first must be 0, 1 or 2");
-    if (o.hot_cache < -1 || o.hot_cache > 64) return fail(DFQ_EINVAL, "hot_cache must be -1, 0 or 1..64 (KB)");
+    if (o.hot_cache < -1 || o.hot_cache > 32) return fail(DFQ_EINVAL, "hot_cache must be -1, 0 or 1..32 (KB)");
     if (o.profile != 0 && o.profile != 1) return fail(DFQ_EINVAL, "profile must be 0 or 1");
     if (o.direction != 0 && o.direction != 1) return fail(DFQ_EINVAL, "direction must be 0 or 1");
     if (o.stall_test_level < 0) return fail(DFQ_EINVAL, "stall_test_level must be >= 0");
     if (o.vertex_order < 0 || o.vertex_order > 2) return fail(DFQ_EINVAL, "vertex_order must be 0, 1 or 2");
-    // the cache itself is cut to what fits; the rest of the layout must fit
-    const dfqk::SmemLayout L =
-        dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true, o.hot_cache > 0);
-    const int need = L.bytes;
+    const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true);
+    const int need = L.bytes + (o.hot_cache > 0 ? 4 * dfqk::kHotWordsMax : 0);
     if (need > 227 * 1024)
         return fail(DFQ_EINVAL, "options need %d bytes of shared memory per block (max 232448)", need);
     return DFQ_OK;
@@ -394,13 +390,11 @@ int check_symmetric(dfq_graph* g) {
     return DFQ_OK;
 }
 
-// Shared-memory words of the hot-vertex cache for one launch on g.
-// hot_cache = K > 0: at most K KB (rounded down to 4 KB), cut to what fits
-// beside the rest of the block's layout at the launch's blocks per SM.
-int hot_words_for(const dfq_graph* g, const dfq_opts& o, bool par) {
-    const int blocks = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, 1024 / o.block_threads) : 1024 / o.block_threads;
-    return dfqk::launch_hot_words(o.hot_cache, g->n, o.block_threads, o.local_queue_cap, o.piece_edges, par, blocks,
-                                  g->sm_smem, g->block_smem);
+// Shared-memory words of the hot-vertex cache for a graph of bitmap_words.
+// hot_cache = K > 0: a cache of K KB (rounded down to 4 KB, at most 32 KB)
+int hot_words_for(const dfq_opts& o, int n) {
+    const int words = dfqk::hot_limit_words(o.hot_cache);
+    return words > 0 ? dfqk::hot_words_of(words, n) : 0;
 }
 
 // Queue control-block reset + the cooperative kernel on g->stream.  The
@@ -412,9 +406,8 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
     const bool par = parents != nullptr;
     KernelFn k = pick_kernel(o.block_threads, par);
     if (!k) return fail(DFQ_EINVAL, "no kernel for block_threads=%d", o.block_threads);
-    const int hot_words = hot_words_for(g, o, par);
-    const dfqk::SmemLayout lay =
-        dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par, hot_words > 0);
+    const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
+    const int hot_words = hot_words_for(o, g->n);
     const int smem = lay.bytes + 4 * hot_words;
     // the limit is shared with every other caller of this kernel
     if (int rc = allow_dyn_smem((const void*)k, smem)) return rc;
@@ -458,7 +451,6 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
     p.use_tma = o.use_tma;
     p.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     p.hot_words = hot_words;
-    p.cold = hot_words > 0;
     p.profile = o.profile;
     if (o.direction == 1 && !g->symmetric)
         return fail(DFQ_EINVAL, "direction = 1 needs a graph created with direction = 1 (checked undirected)");
@@ -548,6 +540,8 @@ int allow_dyn_smem(const void* fn, int smem_needed) {
 
 int device_status(const dfqk::Control& c) { return map_device_status(c); }
 
+int check_opts(const dfq_opts& o) { return validate_opts(o); }
+
 const void* single_source_kernel(int block_threads, bool par) {
     return (const void*)pick_kernel(block_threads, par);
 }
@@ -615,8 +609,6 @@ int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int
     if (err != cudaSuccess) { release(g); return fail(DFQ_ECUDA, "no CUDA device: %s", cudaGetErrorString(err)); }
     if (!prop.cooperativeLaunch) { release(g); return fail(DFQ_ECUDA, "device does not support cooperative launch"); }
     g->sms = prop.multiProcessorCount;
-    g->sm_smem = (int)prop.sharedMemPerMultiprocessor;
-    g->block_smem = (int)prop.sharedMemPerBlockOptin;
 #define G_TRY(x) do { int rc_ = (x); if (rc_) { release(g); return rc_; } } while (0)
 #define G_CUDA(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { release(g); return fail(DFQ_ECUDA, "%s: %s", #x, cudaGetErrorString(e_)); } } while (0)
     G_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
@@ -701,6 +693,7 @@ int dfq_graph_set_opts(dfq_graph* g, const dfq_opts* o) {
 void* dfq_graph_stream(dfq_graph* g) { return g ? (void*)g->stream : nullptr; }
 
 int32_t dfq_graph_num_vertices(const dfq_graph* g) { return g ? g->n : -1; }
+int32_t dfq_graph_is_hub_first(const dfq_graph* g) { return g ? (g->relabeled ? 1 : 0) : -1; }
 int64_t dfq_graph_num_edges(const dfq_graph* g) { return g ? g->e : -1; }
 
 int dfq_bfs_launch(dfq_graph* g, int32_t src, int32_t* levels_dev, int32_t* parents_dev) {

@@ -45,9 +45,31 @@ struct BatchParams {
     int medium_min, large_min, piece_edges, local_cap, local_budget, probe_first, use_tma;
     long long timeout_ns;
     int hot_words;  // hot-vertex cache words this launch reserves (0: none)
-    int cold;       // 1: the launch's layout has cold rings (whenever hot_words > 0)
-    int reserve;    // blocks that run narrow queries during the wide phase
+    int reserve;    // blocks that skip the wide phase (the gangs, then narrow starters)
+    // gangs: the last n_gangs * gang_size blocks form n_gangs fixed groups of
+    // gang_size blocks; each gang runs the gang queries (large high-diameter
+    // graphs, costliest first) one after another from the launch's start,
+    // then its blocks pull narrow queries like the others
+    const int* gang_list;
+    int n_gang;
+    int* gang_next;                 // cursor over gang_list
+    unsigned long long* gang_word;  // per gang: (round << 32) | (query + 1), set by its first block
+    int n_gangs, gang_size;
+    unsigned char* gang_ws;         // per-gang workspaces, gang_ws_stride bytes apart
+    size_t gang_ws_stride;
+    WsLayout gang_lay;
 };
+
+// Published-query word of a gang: release store by the gang's first block,
+// acquire loads by every member.
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 
 __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, int qi, const Workspace& ws) {
     const BatchQuery& q = bp.queries[qi];
@@ -79,7 +101,6 @@ __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, i
     sp.use_tma = bp.use_tma;
     sp.timeout_ns = bp.timeout_ns;
     sp.hot_words = hot_words_of(bp.hot_words, g.n);
-    sp.cold = bp.cold;
     remap_params(sp, g, ws);  // renumbered graphs are wide: only the grid's workspace has room
 }
 
@@ -102,9 +123,29 @@ __device__ __forceinline__ Workspace block_workspace(const BatchParams& bp) {
     return bw;
 }
 
-// Wide queries first, one after another on the whole grid; then every block
-// pulls narrow queries and runs each alone.  One call site of bfs_run (the
-// group shape is chosen per query) keeps the kernel to one inlined copy.
+// This gang's workspace.
+__device__ __forceinline__ Workspace gang_workspace(const BatchParams& bp, int gang) {
+    Workspace gw;
+    unsigned char* base = bp.gang_ws + bp.gang_ws_stride * gang;
+    const WsLayout& l = bp.gang_lay;
+    gw.bitmap = (unsigned*)(base + l.bitmap);
+    for (int i = 0; i < 2; ++i) {
+        gw.ovf[i] = (int2*)(base + l.ovf[i]);
+        gw.ovfv[i] = (int*)(base + l.ovfv[i]);
+        gw.piece[i] = (int2*)(base + l.piece[i]);
+        gw.piece_v[i] = (int*)(base + l.piece_v[i]);
+    }
+    gw.piece_cap = l.piece_cap;
+    gw.levels_int = nullptr;  // gang queries are narrow graphs, kept in input ids
+    gw.parents_int = nullptr;
+    gw.hub_claim = nullptr;
+    return gw;
+}
+
+// Gangs run the gang queries from the launch's start; wide queries run one
+// after another on the wide blocks; then every block pulls narrow queries
+// and runs each alone.  One call site of bfs_run (the group shape is chosen
+// per query) keeps the kernel to one inlined copy.
 template <int B, bool PAR>
 __global__ void __launch_bounds__(B, 1024 / B) dfq_batch_kernel(const __grid_constant__ BatchParams bp) {
     __shared__ Params sp;
@@ -112,36 +153,81 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_batch_kernel(const __grid_con
     init_warp_barriers<B, PAR>(bp.local_cap, bp.piece_edges);
     WarpState ws{0u, false};
     if (blockIdx.x == 0 && threadIdx.x == 0) *bp.t0 = (long long)globaltimer();
-    // the last `reserve` blocks skip the wide queries and start on the narrow
-    // ones (costliest first) at once, so the longest narrow runs overlap the
-    // wide phase instead of trailing it; the wide queries run on the others
+    // the last `reserve` blocks skip the wide queries: first the gangs, then
+    // blocks that start on the narrow ones (costliest first) at once, so the
+    // longest narrow runs overlap the wide phase instead of trailing it; the
+    // wide queries run on the others
     const int wide_blocks = (int)gridDim.x - bp.reserve;
     const bool in_wide = (int)blockIdx.x < wide_blocks;
-    for (int k = in_wide ? 0 : bp.n_wide;; ++k) {
+    const int gang_rel = (int)blockIdx.x - ((int)gridDim.x - bp.n_gangs * bp.gang_size);
+    int gang = -1, gang_rank = 0;  // this block's gang and its rank there (-1: none)
+    if (bp.n_gangs > 0 && gang_rel >= 0) {
+        gang = gang_rel / bp.gang_size;
+        gang_rank = gang_rel % bp.gang_size;
+    }
+    // Gang phase first (gang blocks): the gang's first block takes the next
+    // gang query and publishes it; every member waits for the publication
+    // (bounded), then the gang runs the query with its blocks as the group.
+    // A member reads a round's word before that run's first group barrier,
+    // and the first block publishes the next round only after the run, so no
+    // round is missed.  Then wide queries (wide blocks), then narrow pulls.
+    // Only thread 0 keeps the schedule state.
+    bool gang_phase = gang >= 0;
+    unsigned round = 0;
+    int k = in_wide ? 0 : bp.n_wide;
+    for (;;) {
         if (threadIdx.x == 0) {
-            if (k < bp.n_wide) {
-                s_q = bp.wide_list[k];
-                s_gsize = wide_blocks;
-                s_grank = (int)blockIdx.x;
-                fill_params(sp, bp, s_q, bp.wide_ws);
-                if (blockIdx.x == 0) bp.queries[s_q].t_start = (long long)globaltimer();
-            } else {
-                const int j = atomicAdd(bp.narrow_next, 1);
-                s_q = j < bp.n_narrow ? bp.narrow_list[j] : -1;
-                s_gsize = 1;
-                s_grank = 0;
-                if (s_q >= 0) {
-                    fill_params(sp, bp, s_q, block_workspace(bp));
-                    bp.queries[s_q].t_start = (long long)globaltimer();
+            s_q = -1;
+            if (gang_phase) {
+                ++round;
+                unsigned long long* word = bp.gang_word + gang;
+                if (gang_rank == 0) {
+                    const int j = atomicAdd(bp.gang_next, 1);
+                    const int q = j < bp.n_gang ? bp.gang_list[j] : -1;
+                    st_release_u64(word, ((unsigned long long)round << 32) | (unsigned)(q + 1));
+                }
+                unsigned long long w = ld_acquire_u64(word);
+                const unsigned long long t_wait = globaltimer();
+                while ((unsigned)(w >> 32) != round) {
+                    if ((long long)(globaltimer() - t_wait) > bp.timeout_ns) break;  // leave the gang
+                    w = ld_acquire_u64(word);
+                }
+                const int q = (unsigned)(w >> 32) == round ? (int)(unsigned)w - 1 : -1;
+                if (q >= 0) {
+                    s_q = q;
+                    s_gsize = bp.gang_size;
+                    s_grank = gang_rank;
+                    fill_params(sp, bp, q, gang_workspace(bp, gang));
+                    if (gang_rank == 0) bp.queries[q].t_start = (long long)globaltimer();
+                } else {
+                    gang_phase = false;
+                }
+            }
+            if (!gang_phase && s_q < 0) {
+                if (k < bp.n_wide) {
+                    s_q = bp.wide_list[k++];
+                    s_gsize = wide_blocks;
+                    s_grank = (int)blockIdx.x;
+                    fill_params(sp, bp, s_q, bp.wide_ws);
+                    if (blockIdx.x == 0) bp.queries[s_q].t_start = (long long)globaltimer();
+                } else {
+                    const int j = atomicAdd(bp.narrow_next, 1);
+                    s_q = j < bp.n_narrow ? bp.narrow_list[j] : -1;
+                    s_gsize = 1;
+                    s_grank = 0;
+                    if (s_q >= 0) {
+                        fill_params(sp, bp, s_q, block_workspace(bp));
+                        bp.queries[s_q].t_start = (long long)globaltimer();
+                    }
                 }
             }
         }
         __syncthreads();
         const int qi = s_q;
         if (qi < 0) break;
-        const int gsize = s_gsize;
-        bfs_run<B, PAR>(sp, gsize, s_grank, ws);
-        if (threadIdx.x == 0 && (gsize == 1 || blockIdx.x == 0)) bp.queries[qi].t_end = (long long)globaltimer();
+        bfs_run<B, PAR>(sp, s_gsize, s_grank, ws);
+        // the group's first block records the end (block 0 for wide queries)
+        if (threadIdx.x == 0 && s_grank == 0) bp.queries[qi].t_end = (long long)globaltimer();
         __syncthreads();
     }
 }
@@ -168,6 +254,38 @@ int ensure_blocks(dfq_pool* p, int grid, bool par) {
     p->block_n = (int)nmax;
     p->block_par = par;
     return dmalloc(&p->block_mem, p->block_stride * (size_t)grid);
+}
+
+// Gangs: a narrow graph with at least kGangMinVertices vertices and an
+// average degree below kGangMaxDegree (a high-diameter graph: a grid, a
+// road-like mesh) runs thousands of levels; on one block each level is slow
+// (a few warps carry its whole frontier), so such queries get a gang of
+// blocks when the batch leaves enough of them: the gang budget is a quarter
+// of the grid, shared evenly (at most kGangMax blocks per gang, at most
+// kGangsMax gangs); with fewer than 2 blocks per query they stay narrow.
+constexpr int32_t kGangMinVertices = 1 << 16;
+constexpr int kGangMaxDegree = 8;
+constexpr int kGangMax = 16;
+constexpr int kGangsMax = 24;  // gang words live in the 256-byte misc block, from byte 64
+
+bool gang_graph(const dfq_pool* p, int graph) {
+    return !p->wide[graph] && p->n[graph] >= kGangMinVertices &&
+           p->e[graph] < (int64_t)kGangMaxDegree * p->n[graph];
+}
+
+// (Re)allocate `gangs` gang workspaces for the largest gang graph.
+int ensure_gangs(dfq_pool* p, int gangs, bool par) {
+    long long nmax = 1, emax = 0;
+    for (int i = 0; i < p->ngraphs; ++i)
+        if (gang_graph(p, i)) { nmax = std::max<long long>(nmax, p->n[i]); emax = std::max<long long>(emax, p->e[i]); }
+    if (p->gang_mem && p->gang_count >= gangs && (p->gang_par || !par)) return DFQ_OK;
+    cudaFree(p->gang_mem);
+    p->gang_mem = nullptr;
+    p->gang_lay = ws_layout(nmax, emax, kMinLarge, kMinPiece, par);
+    p->gang_stride = al256(p->gang_lay.total);
+    p->gang_count = gangs;
+    p->gang_par = par;
+    return dmalloc(&p->gang_mem, p->gang_stride * (size_t)std::max(gangs, 1));
 }
 
 int ensure_tables(dfq_pool* p, int nq) {
@@ -254,8 +372,6 @@ int dfq_pool_create(const dfq_csr* graphs, int32_t ngraphs, const dfq_opts* opts
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, p->device) != cudaSuccess) { pool_release(p); return fail(DFQ_ECUDA, "no CUDA device"); }
     p->sms = prop.multiProcessorCount;
-    p->sm_smem = (int)prop.sharedMemPerMultiprocessor;
-    p->block_smem = (int)prop.sharedMemPerBlockOptin;
     int64_t tot_n = 0, tot_e = 0;
     std::vector<int64_t> off_base(ngraphs), col_base(ngraphs);
     for (int i = 0; i < ngraphs; ++i) {
@@ -356,6 +472,92 @@ int dfq_pool_destroy(dfq_pool* p) {
 
 int32_t dfq_pool_num_graphs(const dfq_pool* p) { return p ? p->ngraphs : -1; }
 
+int dfq_pool_get_opts(const dfq_pool* p, dfq_opts* o) {
+    clear_error();
+    if (!p || !o) return fail(DFQ_EINVAL, "dfq_pool_get_opts: null argument");
+    *o = p->opts;
+    return DFQ_OK;
+}
+
+int dfq_pool_set_opts(dfq_pool* p, const dfq_opts* o) {
+    clear_error();
+    if (!p || !o) return fail(DFQ_EINVAL, "dfq_pool_set_opts: null argument");
+    dfq_opts v = *o;
+    if (v.wide_min_edges <= 0) v.wide_min_edges = 1 << 21;
+    if (v.wide_min_degree <= 0) v.wide_min_degree = 8;
+    if (v.block_threads == 0) v.block_threads = 512;
+    if (v.local_queue_cap == 0) v.local_queue_cap = 256;
+    if (v.local_edge_budget == 0) v.local_edge_budget = 8192;
+    if (v.timeout_ms == 0) v.timeout_ms = 5000;
+    if (v.wide_min_edges != p->opts.wide_min_edges || v.wide_min_degree != p->opts.wide_min_degree ||
+        v.vertex_order != p->opts.vertex_order)
+        return fail(DFQ_EINVAL, "dfq_pool_set_opts: wide_min_edges, wide_min_degree and vertex_order are fixed at "
+                    "pool creation (they decided how the graphs were stored)");
+    if (v.direction != 0 || v.stall_test_level != 0)
+        return fail(DFQ_EINVAL, "dfq_pool_set_opts: pools run top-down levels without test hooks");
+    if (int rc = check_opts(v)) return rc;
+    cudaSetDevice(p->device);
+    cudaStreamSynchronize(p->stream);
+    p->opts = v;
+    if (p->gexec) {  // the captured launch baked in the old options
+        cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+        p->g_nq = -1;
+    }
+    return DFQ_OK;
+}
+
+int dfq_pool_autotune(dfq_pool* p, const dfq_query* q, int32_t nq, dfq_opts* best) {
+    clear_error();
+    if (!p || !q || nq < 1 || !best) return fail(DFQ_EINVAL, "dfq_pool_autotune: bad arguments");
+    dfq_opts cur = p->opts;
+    const dfq_opts start = cur;
+    // median of three timed batches (after one untimed) with options o; < 0 on failure
+    auto time_batch = [&](const dfq_opts& o) -> double {
+        if (dfq_pool_set_opts(p, &o) != DFQ_OK) return -1;
+        float ms = 0;
+        if (dfq_pool_batch(p, q, nq, 0, nullptr, &ms) != DFQ_OK) return -1;
+        float t[3];
+        for (float& x : t)
+            if (dfq_pool_batch(p, q, nq, 0, nullptr, &x) != DFQ_OK) return -1;
+        std::sort(t, t + 3);
+        return t[1];
+    };
+    double best_t = time_batch(cur);
+    if (best_t < 0) {
+        dfq_pool_set_opts(p, &start);
+        return fail(DFQ_ECUDA, "dfq_pool_autotune: baseline batch failed");
+    }
+    struct Axis { int32_t dfq_opts::*field; std::vector<int32_t> values; };
+    // kernel options only: the wide split and the vertex order are the pool's
+    const std::vector<Axis> axes = {
+        {&dfq_opts::block_threads, {512, 1024}},
+        {&dfq_opts::medium_min_degree, {16, 32, 64, 128}},
+        {&dfq_opts::large_min_degree, {128, 256, 512, 1024}},
+        {&dfq_opts::piece_edges, {256, 512}},
+        {&dfq_opts::local_queue_cap, {256, 512}},
+        {&dfq_opts::probe_first, {1, 2}},
+        {&dfq_opts::use_tma, {0, 1}},
+    };
+    for (int pass = 0; pass < 2; ++pass) {
+        bool improved = false;
+        for (const Axis& ax : axes)
+            for (int32_t v : ax.values) {
+                if (cur.*ax.field == v) continue;
+                dfq_opts t = cur;
+                t.*ax.field = v;
+                if (t.medium_min_degree > t.large_min_degree) t.medium_min_degree = t.large_min_degree;
+                const double ms = time_batch(t);
+                if (ms > 0 && ms < best_t * 0.98) { best_t = ms; cur = t; improved = true; }
+            }
+        if (!improved) break;
+    }
+    int rc = dfq_pool_set_opts(p, &cur);
+    if (rc) return rc;
+    *best = cur;
+    return DFQ_OK;
+}
+
 int dfq_pool_graph_info(const dfq_pool* p, int32_t graph, int32_t* n, int64_t* e, int32_t* wide) {
     clear_error();
     if (!p || graph < 0 || graph >= p->ngraphs) return fail(DFQ_EINVAL, "dfq_pool_graph_info: bad graph");
@@ -376,8 +578,8 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     const dfq_opts& o = p->opts;
     const void* fn = single_source_kernel(o.block_threads, par);
     if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
-    const int hot = hot_words_of(pool_hot_words(p, par), p->n[graph]);
-    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par, hot > 0);
+    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
+    const int hot = hot_limit_words(o.hot_cache) > 0 ? hot_words_of(hot_limit_words(o.hot_cache), p->n[graph]) : 0;
     const int smem = lay.bytes + 4 * hot;
     int grid = 0;
     if ((rc = grid_for(p, fn, o.block_threads, smem, &grid))) return rc;
@@ -410,7 +612,6 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     prm.use_tma = o.use_tma;
     prm.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     prm.hot_words = hot;
-    prm.cold = hot > 0;
     remap_params(prm, p->h_graphs[graph], w);
     cudaEventRecord(p->ev0, p->stream);
     cudaMemsetAsync(p->d_ctl1, 0, sizeof(Control), p->stream);
@@ -451,10 +652,12 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     const dfq_opts& o = p->opts;
     const void* fn = pick_batch(o.block_threads, par);
     if (!fn) return fail(DFQ_EINVAL, "block_threads %d", o.block_threads);
+    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
     // one cache size per pool (the largest graph's), so a captured launch
-    // stays valid for any batch of the same shape; the cache only on request
-    const int hot = pool_hot_words(p, par);
-    const SmemLayout lay = smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par, hot > 0);
+    // stays valid for any batch of the same shape
+    int hot = 0;
+    if (hot_limit_words(o.hot_cache) > 0)  // the cache only on request
+        for (int i = 0; i < p->ngraphs; ++i) hot = std::max(hot, hot_words_of(hot_limit_words(o.hot_cache), p->n[i]));
     const int smem = lay.bytes + 4 * hot;
     int grid = 0, rc;
     if ((rc = grid_for(p, fn, o.block_threads, smem, &grid))) return rc;
@@ -463,7 +666,7 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     if ((rc = ensure_tables(p, nq))) return rc;
     // query table and lists (pinned staging, copied inside the launch sequence)
     int nw = 0, nn = 0;
-    std::vector<int> narrow;
+    std::vector<int> narrow, ganged;
     for (int i = 0; i < nq; ++i) {
         BatchQuery& b = p->h_queries[i];
         b.graph = q[i].graph;
@@ -472,12 +675,30 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
         b.parents = q[i].parents;
         b.t_start = b.t_end = 0;
         if (p->wide[q[i].graph]) p->h_lists[nw++] = i;
+        else if (gang_graph(p, q[i].graph)) ganged.push_back(i);
         else narrow.push_back(i);
     }
-    std::stable_sort(narrow.begin(), narrow.end(),
-                     [&](int a, int b) { return p->cost[q[a].graph] > p->cost[q[b].graph]; });
+    // gang size: the gang budget (a quarter of the grid) shared by the gang
+    // queries; below 2 blocks per query they run narrow like the rest
+    int gang_size = 0, n_gangs = 0;
+    if (!ganged.empty()) {
+        gang_size = std::min(kGangMax, (grid / 4) / (int)ganged.size());
+        if (gang_size >= 2) {
+            n_gangs = std::min<int>({(int)ganged.size(), (grid / 4) / gang_size, kGangsMax});
+        } else {
+            narrow.insert(narrow.end(), ganged.begin(), ganged.end());
+            ganged.clear();
+            gang_size = 0;
+        }
+    }
+    auto by_cost = [&](int a, int b) { return p->cost[q[a].graph] > p->cost[q[b].graph]; };
+    std::stable_sort(narrow.begin(), narrow.end(), by_cost);
+    std::stable_sort(ganged.begin(), ganged.end(), by_cost);
     nn = (int)narrow.size();
+    const int ng = (int)ganged.size();
     for (int k = 0; k < nn; ++k) p->h_lists[nq + k] = narrow[k];
+    for (int k = 0; k < ng; ++k) p->h_lists[nq + nn + k] = ganged[k];
+    if (n_gangs > 0 && (rc = ensure_gangs(p, n_gangs, par))) return rc;
 
     BatchParams bp;
     memset(&bp, 0, sizeof bp);
@@ -503,11 +724,22 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     bp.use_tma = o.use_tma;
     bp.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     bp.hot_words = hot;
-    bp.cold = hot > 0;
-    // a sixth of the grid starts the narrow queries while the rest runs the
+    // gangs: the last n_gangs * gang_size blocks
+    bp.gang_list = p->d_lists + nq + nn;
+    bp.n_gang = ng;
+    bp.gang_next = p->d_misc + 1;
+    bp.gang_word = reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(p->d_misc) + 64);
+    bp.n_gangs = n_gangs;
+    bp.gang_size = n_gangs > 0 ? gang_size : 1;
+    bp.gang_ws = p->gang_mem;
+    bp.gang_ws_stride = p->gang_stride;
+    bp.gang_lay = p->gang_lay;
+    // a sixth of the rest starts the narrow queries while the others run the
     // wide ones (when there are both; measured on the 256-graph pool: 1/16
     // 16.1k, 1/8 17.0-18.0k, 1/6 18.1k, 1/4 17.1k queries/s)
-    bp.reserve = (nw > 0 && nn > 0) ? std::min(nn, std::max(1, grid / 6)) : 0;
+    const int gang_blocks = n_gangs * gang_size;
+    const int rest = grid - gang_blocks;
+    bp.reserve = gang_blocks + ((nw > 0 && nn > 0) ? std::min(nn, std::max(1, rest / 6)) : 0);
 
     auto enqueue = [&]() -> int {
         cudaError_t e1 = cudaMemcpyAsync(p->d_queries, p->h_queries, sizeof(BatchQuery) * nq, cudaMemcpyHostToDevice, p->stream);
@@ -521,7 +753,8 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
     if (flags & DFQ_BATCH_GRAPH) {
         // the captured graph bakes in the kernel arguments: rebuild it when
         // the batch's shape changes, else replay it with new table contents
-        if (!p->gexec || p->g_nq != nq || p->g_nwide != nw || p->g_par != (int)par) {
+        if (!p->gexec || p->g_nq != nq || p->g_nwide != nw || p->g_par != (int)par || p->g_nnarrow != nn ||
+            p->g_gangs != n_gangs || p->g_gang_size != gang_size) {
             if (p->gexec) { cudaGraphExecDestroy(p->gexec); p->gexec = nullptr; }
             cudaGraph_t graph = nullptr;
             cudaError_t err = cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal);
@@ -536,6 +769,9 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
             p->g_nq = nq;
             p->g_nwide = nw;
             p->g_par = par;
+            p->g_nnarrow = nn;
+            p->g_gangs = n_gangs;
+            p->g_gang_size = gang_size;
         }
         cudaError_t err = cudaGraphLaunch(p->gexec, p->stream);
         if (err != cudaSuccess) return fail(DFQ_ECUDA, "graph launch: %s", cudaGetErrorString(err));

@@ -123,10 +123,6 @@ struct Params {
     // visited bits of vertices [0, 32 * hot_words) cached in shared memory on
     // probe levels (0: no cache); a multiple of 32 words, at most kHotWordsMax
     int hot_words;
-    // 1: the launch reserved per-warp cold rings (shared-memory layout with
-    // cold = true); required whenever hot_words > 0, the same for every
-    // query of one launch
-    int cold;
     int profile;  // 1: record each block's level finish times
     int direction;  // 1: levels may run bottom-up (undirected graph, checked by the host)
     int e;          // edges (the bottom-up switch compares against the unexplored ones)
@@ -351,13 +347,7 @@ __device__ __forceinline__ bool group_barrier(Control* ctl, int gsize, unsigned&
 
 // ------------------------------------------------------------ shared layout
 constexpr int kRing = 256;  // per-warp candidate ring (entries, power of two)
-// per-warp ring of probes the hot-vertex cache could not settle (entries,
-// power of two); probed against the global bitmap kColdBatch at a time, eight
-// loads per lane in flight together.  It holds < kColdBatch entries between
-// calls and one call appends at most 256, so it never wraps onto pending ones.
-constexpr int kCold = 512;
-constexpr int kColdBatch = 256;
-constexpr int kHotWordsMax = 16384;  // hot-vertex visited cache: at most 64 KB, 524,288 vertices
+constexpr int kHotWordsMax = 8192;  // hot-vertex visited cache: 32 KB, 262,144 vertices
 
 // Words of a hot-vertex cache of `kb` KB (0 if kb <= 0), rounded down to 4 KB,
 // at most kHotWordsMax.
@@ -379,13 +369,10 @@ struct SmemLayout {
     int ring_off;  // per-warp candidate ring: kRing vertices (+ kRing parents)
     int tma_off;   // per-warp piece buffers: 2 x (piece + 16) ints, 128-byte aligned
     int bar_off;   // per-warp mbarriers: 2 x u64
-    int cold_off;  // per-warp cold rings: kCold vertices (+ kCold parents), with cold only
     int hot_off;   // hot-vertex visited cache (last, so its size changes no other offset)
     int bytes;     // without the hot cache: a launch adds 4 * hot_words
 };
-// cold: the launch keeps a hot-vertex cache, so each warp also gets a cold ring
-// (placed after the mbarriers, so the barrier addresses do not depend on it).
-__host__ __device__ inline SmemLayout smem_layout(int B, int cap, int piece, bool par, bool cold = false) {
+__host__ __device__ inline SmemLayout smem_layout(int B, int cap, int piece, bool par) {
     SmemLayout L;
     const int NW = B / 32;
     int o = 0;
@@ -397,38 +384,9 @@ __host__ __device__ inline SmemLayout smem_layout(int B, int cap, int piece, boo
     o = (o + 15) & ~15;
     L.bar_off = o;  o += NW * 2 * 8;
     o = (o + 15) & ~15;
-    L.cold_off = o;
-    if (cold) o += NW * kCold * (par ? 2 : 1) * 4;
     L.hot_off = o;
     L.bytes = o;
     return L;
-}
-
-// Largest hot-vertex cache (words, a multiple of 1024, at most kHotWordsMax)
-// that fits next to layout bytes in smem_limit bytes of shared memory.
-__host__ __device__ inline int hot_fit_words(int layout_bytes, int smem_limit) {
-    int w = ((smem_limit - layout_bytes) / 4) & ~1023;
-    if (w < 0) w = 0;
-    return w < kHotWordsMax ? w : kHotWordsMax;
-}
-
-// Hot-vertex cache words of a launch: the hot_cache_kb KB asked for, cut to
-// what fits beside the layout with cold rings when `blocks` blocks share an
-// SM's sm_smem bytes (each block at most block_max, minus the 1 KB the
-// system reserves per block), and to the bitmap of a graph of n_max
-// vertices; 0 when that leaves less than 4 KB (then no cold rings either).
-inline int launch_hot_words(int hot_cache_kb, long long n_max, int B, int cap, int piece, bool par, int blocks,
-                            int sm_smem, int block_max) {
-    const int want = hot_limit_words(hot_cache_kb);
-    if (want <= 0) return 0;
-    if (blocks < 1) blocks = 1;
-    const SmemLayout L = smem_layout(B, cap, piece, par, true);
-    int per_block = sm_smem / blocks - 1024;
-    if (per_block > block_max) per_block = block_max;
-    int w = hot_fit_words(L.bytes, per_block);
-    if (w > want) w = want;
-    w = hot_words_of(w, n_max > (1LL << 30) ? (1 << 30) : (int)n_max);
-    return w >= 1024 ? w : 0;
 }
 
 
@@ -747,7 +705,7 @@ __device__ __forceinline__ void visit4(const Params& p, const Lv& lv, Tally& t, 
 // mean fewer pushes, so fewer atomics on the level's counters.
 // Warp-collective.
 template <bool PAR>
-__device__ __forceinline__ void ring_drain_body(const Params& p, const Lv& lv, Tally& t, Ring& r, bool all) {
+__device__ __forceinline__ void ring_drain(const Params& p, const Lv& lv, Tally& t, Ring& r, bool all) {
     const int lane = threadIdx.x & 31;
     while (r.n >= 128 || (all && r.n > 0)) {
         const int take = r.n < 128 ? r.n : 128;
@@ -772,140 +730,17 @@ __device__ __forceinline__ void ring_drain_body(const Params& p, const Lv& lv, T
     }
 }
 
-// The drain above as one out-of-line copy per kernel: it runs once per 128
-// candidates, so a call costs little, while inlining it at every probe site
-// multiplied the kernel's code (and its compile time) several times over.
-// Ring state and the claim count travel by value.
-struct RingOut {
-    int head;
-    int n;
-    unsigned claims;
-};
-template <bool PAR>
-__device__ __noinline__ RingOut ring_drain_call(const Params& p, Lv lv, int* rv, int head, int n, bool all) {
-    Ring r;
-    r.v = rv;
-    r.head = head;
-    r.n = n;
-    Tally t{0u, 0u};
-    ring_drain_body<PAR>(p, lv, t, r, all);
-    return RingOut{r.head, r.n, t.claims};
-}
-template <bool PAR>
-__device__ __forceinline__ void ring_drain(const Params& p, const Lv& lv, Tally& t, Ring& r, bool all) {
-    if (!(r.n >= 128 || (all && r.n > 0))) return;
-    const RingOut o = ring_drain_call<PAR>(p, lv, r.v, r.head, r.n, all);
-    r.head = o.head;
-    r.n = o.n;
-    t.claims += o.claims;
-}
-
-// Append the entries of v selected by m (bit j: v[j], with parent par[j]) to
-// ring r of capacity CAP (a power of two; parents stored CAP entries after
-// the vertices) by a prefix-sum compaction; the caller guarantees room.
-// Returns how many were appended (warp-uniform).  Warp-collective.
-template <bool PAR, int CAP, int K>
-__device__ __forceinline__ int ring_append(Ring& r, const int (&v)[K], unsigned m, const int (&par)[K]) {
-    const int lane = threadIdx.x & 31;
-    const int c = __popc(m);
-    int incl = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int tt = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += tt;
-    }
-    const int tot = __shfl_sync(kFull, incl, 31);
-    if (tot == 0) return 0;
-    int pos = r.head + r.n + incl - c;
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-        if (m >> j & 1) {
-            const int idx = pos & (CAP - 1);
-            r.v[idx] = v[j];
-            if (PAR) r.v[CAP + idx] = par[j];
-            ++pos;
-        }
-    }
-    __syncwarp();
-    r.n += tot;
-    return tot;
-}
-
-// Probe the cold ring against the global bitmap, kColdBatch entries at a
-// time (eight loads per lane, all in flight together), while a full batch is
-// waiting, or until the ring is empty when `all`.  Unvisited entries go to
-// the candidate ring in two halves of at most 128 with a claim drain between
-// (the candidate ring holds < 128 between calls).  Warp-collective.
-template <bool PAR>
-__device__ __forceinline__ void cold_drain(const Params& p, const Lv& lv, Tally& t, Ring& r, Ring& cold, bool all) {
-    const int lane = threadIdx.x & 31;
-    while (cold.n >= kColdBatch || (all && cold.n > 0)) {
-        const int take = cold.n < kColdBatch ? cold.n : kColdBatch;
-        int v[8], par[8];
-        unsigned vm = 0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            v[j] = 0;
-            par[j] = 0;
-            const int k = j * 32 + lane;
-            if (k < take) {
-                const int idx = (cold.head + k) & (kCold - 1);
-                v[j] = cold.v[idx];
-                if (PAR) par[j] = cold.v[kCold + idx];
-                vm |= 1u << j;
-            }
-        }
-        __syncwarp();
-        cold.head = (cold.head + take) & (kCold - 1);
-        cold.n -= take;
-        unsigned w[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) w[j] = (vm >> j & 1) ? p.bitmap[v[j] >> 5] : 0xffffffffu;
-        unsigned cm = 0;
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if ((vm >> j & 1) && !((w[j] >> (v[j] & 31)) & 1u)) cm |= 1u << j;
-        if (!__any_sync(kFull, cm)) continue;
-        const int lo[4] = {v[0], v[1], v[2], v[3]}, hi[4] = {v[4], v[5], v[6], v[7]};
-        const int plo[4] = {par[0], par[1], par[2], par[3]}, phi[4] = {par[4], par[5], par[6], par[7]};
-        ring_append<PAR, kRing, 4>(r, lo, cm & 15u, plo);
-        ring_drain<PAR>(p, lv, t, r, false);
-        ring_append<PAR, kRing, 4>(r, hi, cm >> 4, phi);
-        ring_drain<PAR>(p, lv, t, r, false);
-    }
-}
-
-// Probe levels with a hot-vertex cache: scanned neighbours (bit j of vm:
-// v[j], parent par[j]) that the shared-memory cache shows visited are done;
-// the rest wait in the cold ring and are probed against the global bitmap a
-// full batch at a time.  A warp then waits for one round of global loads per
-// 256 unsettled probes, instead of one per 128 or 256 scanned edges (a round
-// lasts as long as its slowest load, and nearly every round of raw probes
-// has one that misses L1).  Warp-collective.
-template <bool PAR, int K>
-__device__ __forceinline__ void probe_cold(const Params& p, const Lv& lv, Tally& t, Ring& r, Ring& cold,
-                                           const int (&v)[K], unsigned vm, const int (&par)[K]) {
-    t.edges += __popc(vm);
-    vm = hot_filter<K>(lv, v, vm);
-    if (!__any_sync(kFull, vm)) return;
-    ring_append<PAR, kCold, K>(cold, v, vm, par);
-    cold_drain<PAR>(p, lv, t, r, cold, false);
-}
-
 // Probe levels: test up to four neighbours per lane against the visited
 // bitmap and append the unvisited ones to the warp's ring (prefix-sum
 // compaction); claims happen in batches of 128 in ring_drain.  The ring
 // holds < 128 entries between calls, so one call (<= 128 appends) never
 // wraps onto unclaimed entries.  Warp-collective.
 template <bool PAR>
-__device__ __forceinline__ void probe4(const Params& p, const Lv& lv, Tally& t, Ring& r, Ring& cold,
-                                       const int (&v)[4], unsigned vmask, const int (&par)[4]) {
-    if (lv.hot) {
-        probe_cold<PAR, 4>(p, lv, t, r, cold, v, vmask, par);
-        return;
-    }
+__device__ __forceinline__ void probe4(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[4],
+                                       unsigned vmask, const int (&par)[4]) {
     const int lane = threadIdx.x & 31;
     t.edges += __popc(vmask);
+    vmask = hot_filter<4>(lv, v, vmask);
     unsigned w[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) w[j] = (vmask >> j & 1) ? p.bitmap[v[j] >> 5] : 0xffffffffu;
@@ -943,15 +778,11 @@ __device__ __forceinline__ void probe4(const Params& p, const Lv& lv, Tally& t, 
 // between calls) never holds more than 255.  One scan serves both halves
 // (counts packed in 16-bit fields).  Warp-collective.
 template <bool PAR>
-__device__ __forceinline__ void probe8(const Params& p, const Lv& lv, Tally& t, Ring& r, Ring& cold,
-                                       const int (&v)[8], unsigned vm, int par0) {
-    if (lv.hot) {
-        const int par[8] = {par0, par0, par0, par0, par0, par0, par0, par0};
-        probe_cold<PAR, 8>(p, lv, t, r, cold, v, vm, par);
-        return;
-    }
+__device__ __forceinline__ void probe8(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[8],
+                                       unsigned vm, int par0) {
     const int lane = threadIdx.x & 31;
     t.edges += __popc(vm);
+    vm = hot_filter<8>(lv, v, vm);
     unsigned w[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) w[j] = (vm >> j & 1) ? p.bitmap[v[j] >> 5] : 0xffffffffu;
@@ -992,8 +823,8 @@ __device__ __forceinline__ void probe8(const Params& p, const Lv& lv, Tally& t, 
 // piece's aligned span, the piece itself is [off, tw); lanes take eight
 // consecutive entries (two 16-byte shared-memory reads).  Warp-collective.
 template <bool PAR>
-__device__ __forceinline__ void probe_piece(const Params& p, const Lv& lv, Tally& t, Ring& r, Ring& cold,
-                                            const int* buf, int off, int tw, int par0) {
+__device__ __forceinline__ void probe_piece(const Params& p, const Lv& lv, Tally& t, Ring& r, const int* buf,
+                                            int off, int tw, int par0) {
     const int lane = threadIdx.x & 31;
     for (int base = 0; base < tw; base += 256) {
         const int w8 = base + 8 * lane;
@@ -1005,23 +836,22 @@ __device__ __forceinline__ void probe_piece(const Params& p, const Lv& lv, Tally
 #pragma unroll
         for (int j = 0; j < 8; ++j)
             if (w8 + j >= off && w8 + j < tw) vm |= 1u << j;
-        probe8<PAR>(p, lv, t, r, cold, v, vm, par0);
+        probe8<PAR>(p, lv, t, r, v, vm, par0);
     }
 }
 
 // Probe or claim-at-once, by level.  Warp-collective.
 template <bool PAR>
-__device__ __forceinline__ void scan4(const Params& p, const Lv& lv, Tally& t, Ring& r, Ring& cold,
-                                      const int (&v)[4], unsigned vmask, const int (&par)[4]) {
-    if (lv.probe) probe4<PAR>(p, lv, t, r, cold, v, vmask, par);
+__device__ __forceinline__ void scan4(const Params& p, const Lv& lv, Tally& t, Ring& r, const int (&v)[4],
+                                      unsigned vmask, const int (&par)[4]) {
+    if (lv.probe) probe4<PAR>(p, lv, t, r, v, vmask, par);
     else visit4<PAR>(p, lv, t, v, vmask, par);
 }
 
 // One warp expands one list [s, s+d): int4 column loads from the 16-byte
 // aligned floor of the list; lanes mask what lies outside it.
 template <bool PAR>
-__device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally& t, Ring& r, Ring& cold, int s,
-                                            int d, int u) {
+__device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally& t, Ring& r, int s, int d, int u) {
     const int lane = threadIdx.x & 31;
     const int e0 = s, e1 = s + d;
     const int par[4] = {u, u, u, u};
@@ -1036,7 +866,7 @@ __device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally
                 if (k4 + j >= e0 && k4 + j < e1) vm |= 1u << j;
         }
         const int v[4] = {x.x, x.y, x.z, x.w};
-        scan4<PAR>(p, lv, t, r, cold, v, vm, par);
+        scan4<PAR>(p, lv, t, r, v, vm, par);
     }
 }
 
@@ -1045,8 +875,8 @@ __device__ __forceinline__ void warp_expand(const Params& p, const Lv& lv, Tally
 // gather over the concatenation of their lists (4 edges per lane per round).
 // wl: this warp's 96-int scratch (scan, start, parent).  Warp-collective.
 template <bool PAR>
-__device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tally& t, Ring& r, Ring& cold, int* wl,
-                                             bool has, int s, int d, int u) {
+__device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tally& t, Ring& r, int* wl, bool has,
+                                             int s, int d, int u) {
     const int lane = threadIdx.x & 31;
     if (!has) d = 0;
     const bool med = d >= p.medium_min;
@@ -1054,8 +884,7 @@ __device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tall
     while (mmask) {
         const int i = __ffs(mmask) - 1;
         mmask &= mmask - 1;
-        warp_expand<PAR>(p, lv, t, r, cold, __shfl_sync(kFull, s, i), __shfl_sync(kFull, d, i),
-                         __shfl_sync(kFull, u, i));
+        warp_expand<PAR>(p, lv, t, r, __shfl_sync(kFull, s, i), __shfl_sync(kFull, d, i), __shfl_sync(kFull, u, i));
     }
     const int ds = med ? 0 : d;
     int incl = ds;
@@ -1093,7 +922,7 @@ __device__ __forceinline__ void warp_process(const Params& p, const Lv& lv, Tall
                 vm |= 1u << j;
             }
         }
-        scan4<PAR>(p, lv, t, r, cold, v, vm, par);
+        scan4<PAR>(p, lv, t, r, v, vm, par);
     }
 }
 
@@ -1205,17 +1034,13 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
     // group-wide warp index, interleaved across blocks so that consecutive
     // statically assigned chunks land on different SMs
     const int gwarp = warp * gsize + grank, nwarps = gsize * NW;
-    const SmemLayout lay = smem_layout(B, p.local_cap, p.piece_edges, PAR, p.cold != 0);
+    const SmemLayout lay = smem_layout(B, p.local_cap, p.piece_edges, PAR);
     const int P = p.piece_edges;
     int* wl = reinterpret_cast<int*>(dfq_smem + lay.wl_off) + warp * 96;
     Ring ring;
     ring.v = reinterpret_cast<int*>(dfq_smem + lay.ring_off) + warp * kRing * (PAR ? 2 : 1);
     ring.head = 0;
     ring.n = 0;
-    Ring cold;  // used only on levels with a hot-vertex cache (then p.cold reserved it)
-    cold.v = reinterpret_cast<int*>(dfq_smem + lay.cold_off) + warp * kCold * (PAR ? 2 : 1);
-    cold.head = 0;
-    cold.n = 0;
     int* wbuf0 = reinterpret_cast<int*>(dfq_smem + lay.tma_off) + warp * 2 * (P + 16);
     unsigned long long* wbar = reinterpret_cast<unsigned long long*>(dfq_smem + lay.bar_off) + warp * 2;
     Control* ctl = p.ctl;
@@ -1346,7 +1171,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         // the global bitmap (everything visited before this level) and added
         // to during the level as this block meets visited vertices
         lv.hot = 0u;
-        if (lv.probe && !lv.bottom_up && p.hot_words > 0 && p.cold) {
+        if (lv.probe && !lv.bottom_up && p.hot_words > 0) {
             lv.hot = 32u * (unsigned)p.hot_words;
             const uint4* src4 = reinterpret_cast<const uint4*>(p.bitmap);
             uint4* dst4 = reinterpret_cast<uint4*>(hot_cache());
@@ -1386,8 +1211,8 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                     if (j >= nloc) break;
                     const int i = j + lane;
                     const bool has = lane < grab && i < nloc;
-                    warp_process<PAR>(p, lv, t, ring, cold, wl, has, has ? qc[i] : 0,
-                                      has ? qc[p.local_cap + i] : 0, (PAR && has) ? qc[2 * p.local_cap + i] : 0);
+                    warp_process<PAR>(p, lv, t, ring, wl, has, has ? qc[i] : 0, has ? qc[p.local_cap + i] : 0,
+                                      (PAR && has) ? qc[2 * p.local_cap + i] : 0);
                 }
             }
 
@@ -1413,7 +1238,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                     const int step = (d.y - d.x + split - 1) / split;
                     const int lo = d.x + (g - k * split) * step;
                     const int hi = min(d.y, lo + step);
-                    if (hi > lo) warp_expand<PAR>(p, lv, t, ring, cold, lo, hi - lo, par0);
+                    if (hi > lo) warp_expand<PAR>(p, lv, t, ring, lo, hi - lo, par0);
                 }
             } else if (total_pieces > 0 && !warp_failed) {
                 const int2* pin = p.piece[in];
@@ -1487,7 +1312,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                         const int* buf = wbuf0 + cb * (P + 16);
                         const int a0 = lo & ~3, off = lo - a0, tw = hi - a0;
                         if (lv.probe) {
-                            probe_piece<PAR>(p, lv, t, ring, cold, buf, off, tw, par0);
+                            probe_piece<PAR>(p, lv, t, ring, buf, off, tw, par0);
                         } else {
                             const int par[4] = {par0, par0, par0, par0};
                             for (int base = 0; base < tw; base += 128) {
@@ -1501,11 +1326,11 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                                         if (w4 + j >= off && w4 + j < tw) vm |= 1u << j;
                                 }
                                 const int v[4] = {x.x, x.y, x.z, x.w};
-                                scan4<PAR>(p, lv, t, ring, cold, v, vm, par);
+                                scan4<PAR>(p, lv, t, ring, v, vm, par);
                             }
                         }
                     } else {
-                        warp_expand<PAR>(p, lv, t, ring, cold, lo, hi - lo, par0);
+                        warp_expand<PAR>(p, lv, t, ring, lo, hi - lo, par0);
                     }
                     __syncwarp();
                     cb ^= 1;
@@ -1546,7 +1371,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                         x = __ldcg(ovf_in + i);
                         if (PAR) u = __ldcg(ovfv_in + i);
                     }
-                    warp_process<PAR>(p, lv, t, ring, cold, wl, has, x.x, x.y, u);
+                    warp_process<PAR>(p, lv, t, ring, wl, has, x.x, x.y, u);
                 }
             }
         }
@@ -1555,7 +1380,6 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             if (p.profile && lane == 0 && L < kTraceLevels)
                 atomicMax(&sh.phase_max[2], (unsigned)(globaltimer() - sh.level_t0[warp]));
         }
-        if (lv.hot) cold_drain<PAR>(p, lv, t, ring, cold, true);
         ring_drain<PAR>(p, lv, t, ring, true);
         if (p.profile && lane == 0 && L < kTraceLevels)
             atomicMax(&sh.phase_max[3], (unsigned)(globaltimer() - sh.level_t0[warp]));
@@ -1649,7 +1473,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
 // Per-warp mbarriers, initialised once per launch.
 template <int B, bool PAR>
 __device__ __forceinline__ void init_warp_barriers(int local_cap, int piece) {
-    const SmemLayout lay = smem_layout(B, local_cap, piece, PAR);  // mbarriers sit before the cold rings
+    const SmemLayout lay = smem_layout(B, local_cap, piece, PAR);
     unsigned long long* wbar = reinterpret_cast<unsigned long long*>(dfq_smem + lay.bar_off) + (threadIdx.x >> 5) * 2;
     if ((threadIdx.x & 31) == 0) {
         mbar_init(&wbar[0], 1);

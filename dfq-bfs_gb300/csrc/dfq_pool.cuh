@@ -97,8 +97,6 @@ struct dfq_pool {
     using PoolGraph = dfqk::PoolGraph;
     int device = 0;
     int sms = 0;
-    int sm_smem = 0;     // shared memory per SM (bytes)
-    int block_smem = 0;  // opt-in shared memory per block (bytes)
     dfq_opts opts{};
     int32_t ngraphs = 0;
     std::vector<int32_t> n;
@@ -134,7 +132,13 @@ struct dfq_pool {
     int qcap = 0;
     // captured batch
     cudaGraphExec_t gexec = nullptr;
-    int g_nq = -1, g_nwide = -1, g_par = -1;
+    int g_nq = -1, g_nwide = -1, g_par = -1, g_nnarrow = -1, g_gangs = -1, g_gang_size = -1;
+    // gang workspaces (largest gang graph), gang_count of them
+    unsigned char* gang_mem = nullptr;
+    size_t gang_stride = 0;
+    WsLayout gang_lay{};
+    int gang_count = 0;
+    bool gang_par = false;
     // single-query launches
     Control* d_ctl1 = nullptr;
     Control* h_ctl1 = nullptr;
@@ -171,6 +175,7 @@ inline void pool_release(dfq_pool* p) {
     cudaFree(p->d_graphs);
     cudaFree(p->wide_mem);
     cudaFree(p->block_mem);
+    cudaFree(p->gang_mem);
     cudaFree(p->d_queries);
     cudaFree(p->d_lists);
     cudaFree(p->d_ctls);
@@ -218,17 +223,6 @@ inline int ensure_wide(dfq_pool* p, bool par) {
     p->wide_lay = ws_layout(nmax, emax, kMinLarge, kMinPiece, par, remap);
     p->wide_par = par;
     return dmalloc(&p->wide_mem, p->wide_lay.total);
-}
-
-// Hot-vertex cache words a launch over the pool reserves per block (the
-// largest graph's, cut to what fits; 0 unless the options ask for a cache).
-inline int pool_hot_words(const dfq_pool* p, bool par) {
-    const dfq_opts& o = p->opts;
-    long long nmax = 1;
-    for (int i = 0; i < p->ngraphs; ++i) nmax = std::max<long long>(nmax, p->n[i]);
-    const int blocks = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, 1024 / o.block_threads) : 1024 / o.block_threads;
-    return launch_hot_words(o.hot_cache, nmax, o.block_threads, o.local_queue_cap, o.piece_edges, par, blocks,
-                            p->sm_smem, p->block_smem);
 }
 
 inline int grid_for(dfq_pool* p, const void* fn, int B, int smem, int* grid) {

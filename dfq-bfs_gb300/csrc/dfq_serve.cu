@@ -141,7 +141,6 @@ __device__ __forceinline__ void serve_params(Params& sp, const ServeParams& s, c
     sp.use_tma = s.use_tma;
     sp.timeout_ns = s.timeout_ns;
     sp.hot_words = hot_words_of(s.hot_words, g.n);
-    sp.cold = s.hot_words > 0;  // the launch reserved cold rings with its cache
     remap_params(sp, g, ws);  // renumbered graphs are wide: only the gang's workspace has room
 }
 
@@ -655,9 +654,11 @@ int dfq_server_create(dfq_pool* pool, const dfq_server_opts* opts, dfq_server** 
     const dfq_opts& po = pool->opts;
     s->fn = pick_serve(po.block_threads, par);
     if (!s->fn) { server_release_all(s); return fail(DFQ_EINVAL, "block_threads %d", po.block_threads); }
-    s->hot_words = pool_hot_words(pool, par);  // the cache only on request
-    s->smem = smem_layout(po.block_threads, po.local_queue_cap, po.piece_edges, par, s->hot_words > 0).bytes +
-              4 * s->hot_words;
+    s->hot_words = 0;
+    if (hot_limit_words(po.hot_cache) > 0)  // the cache only on request
+        for (int i = 0; i < pool->ngraphs; ++i)
+            s->hot_words = std::max(s->hot_words, hot_words_of(hot_limit_words(po.hot_cache), pool->n[i]));
+    s->smem = smem_layout(po.block_threads, po.local_queue_cap, po.piece_edges, par).bytes + 4 * s->hot_words;
     S_TRY(grid_for(pool, s->fn, po.block_threads, s->smem, &s->grid));
     S_TRY(ensure_wide(pool, par));
     // narrow workspaces: bitmap for the largest narrow graph, bounded queues

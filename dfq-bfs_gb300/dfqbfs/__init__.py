@@ -42,6 +42,8 @@ EXPORTS = [
     "dfq_pool_batch", "dfq_server_create", "dfq_server_submit", "dfq_server_poll", "dfq_server_levels",
     "dfq_server_release", "dfq_server_pending", "dfq_server_destroy", "dfq_server_replay",
     "dfq_set_host_threads", "dfq_host_threads", "dfq_bfs_last_levels", "dfq_frontier_profile",
+    "dfq_graph_is_hub_first", "dfq_graph_class", "dfq_autotune_cached",
+    "dfq_pool_get_opts", "dfq_pool_set_opts", "dfq_pool_autotune",
 ]
 BATCH_GRAPH = 1
 
@@ -157,6 +159,13 @@ def lib() -> C.CDLL:
     L.dfq_graph_sync.argtypes = [C.c_void_p]
     L.dfq_bfs_last_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     L.dfq_autotune.argtypes = [C.c_void_p, P32, C.c_int32, C.POINTER(Opts)]
+    L.dfq_graph_is_hub_first.argtypes = [C.c_void_p]
+    L.dfq_graph_is_hub_first.restype = C.c_int32
+    L.dfq_graph_class.argtypes = [C.c_void_p, C.c_char_p, C.c_int32]
+    L.dfq_autotune_cached.argtypes = [C.c_void_p, P32, C.c_int32, C.c_char_p, C.POINTER(Opts),
+                                      C.POINTER(C.c_int32)]
+    L.dfq_pool_get_opts.argtypes = [C.c_void_p, C.POINTER(Opts)]
+    L.dfq_pool_set_opts.argtypes = [C.c_void_p, C.POINTER(Opts)]
     L.dfq_pool_create.argtypes = [C.POINTER(_Csr), C.c_int32, C.POINTER(Opts), C.POINTER(C.c_void_p)]
     L.dfq_pool_destroy.argtypes = [C.c_void_p]
     L.dfq_pool_num_graphs.argtypes = [C.c_void_p]
@@ -164,6 +173,7 @@ def lib() -> C.CDLL:
     L.dfq_pool_graph_info.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int64),
                                       C.POINTER(C.c_int32)]
     L.dfq_pool_bfs.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(Stats)]
+    L.dfq_pool_autotune.argtypes = [C.c_void_p, C.POINTER(Query), C.c_int32, C.POINTER(Opts)]
     L.dfq_pool_batch.argtypes = [C.c_void_p, C.POINTER(Query), C.c_int32, C.c_int32, C.POINTER(QueryResult),
                                  C.POINTER(C.c_float)]
     for name in ("dfq_pool_create", "dfq_pool_destroy", "dfq_pool_graph_info", "dfq_pool_bfs", "dfq_pool_batch"):
@@ -461,6 +471,26 @@ class Graph:
         check(lib().dfq_autotune(self.h, _p32(s), len(s), C.byref(o)))
         return o
 
+    @property
+    def hub_first(self) -> bool:
+        return lib().dfq_graph_is_hub_first(self.h) == 1
+
+    def graph_class(self) -> str:
+        buf = C.create_string_buffer(128)
+        k = lib().dfq_graph_class(self.h, buf, len(buf))
+        if k < 0:
+            check(k)
+        return buf.value.decode()
+
+    def autotune_cached(self, sources, cache_path) -> tuple[Opts, bool]:
+        """dfq_autotune_cached: (options installed, True if they came from the cache)."""
+        s = np.ascontiguousarray(sources, dtype=np.int32)
+        o = Opts()
+        hit = C.c_int32()
+        check(lib().dfq_autotune_cached(self.h, _p32(s), len(s), str(cache_path).encode(), C.byref(o),
+                                        C.byref(hit)))
+        return o, bool(hit.value)
+
 
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
@@ -510,6 +540,31 @@ class Pool:
         check(lib().dfq_pool_graph_info(self.h, graph, C.byref(n), C.byref(e), C.byref(w)))
         return n.value, e.value, bool(w.value)
 
+    def opts(self) -> Opts:
+        o = Opts()
+        check(lib().dfq_pool_get_opts(self.h, C.byref(o)))
+        return o
+
+    def set_opts(self, o: Opts) -> None:
+        check(lib().dfq_pool_set_opts(self.h, C.byref(o)))
+
+    @staticmethod
+    def _query_array(queries):
+        qa = (Query * len(queries))()
+        for i, q in enumerate(queries):
+            qa[i].graph, qa[i].source = int(q[0]), int(q[1])
+            qa[i].levels = _ptr(q[2])
+            qa[i].parents = _ptr(q[3]) if len(q) > 3 and q[3] is not None else None
+        return qa
+
+    def autotune(self, queries) -> Opts:
+        """dfq_pool_autotune on these queries (same form as batch()); installs
+        and returns the winning options."""
+        qa = self._query_array(queries)
+        o = Opts()
+        check(lib().dfq_pool_autotune(self.h, qa, len(queries), C.byref(o)))
+        return o
+
     def bfs(self, graph: int, source: int, levels_dev, parents_dev=None) -> Stats:
         st = Stats()
         check(lib().dfq_pool_bfs(self.h, graph, source, _ptr(levels_dev),
@@ -519,11 +574,7 @@ class Pool:
     def batch(self, queries, flags: int = 0, check_status: bool = True):
         """queries: list of (graph, source, levels_dev[, parents_dev]).
         Returns (list of QueryResult, total device ms)."""
-        qa = (Query * len(queries))()
-        for i, q in enumerate(queries):
-            qa[i].graph, qa[i].source = int(q[0]), int(q[1])
-            qa[i].levels = _ptr(q[2])
-            qa[i].parents = _ptr(q[3]) if len(q) > 3 and q[3] is not None else None
+        qa = self._query_array(queries)
         res = (QueryResult * len(queries))()
         ms = C.c_float()
         rc = lib().dfq_pool_batch(self.h, qa, len(queries), flags, res, C.byref(ms))

@@ -283,6 +283,27 @@ int dfq_frontier_profile(const dfq_csr* g, const int32_t* levels, const int32_t 
  * writes the winner to *best and installs it on the graph. */
 int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, dfq_opts* best);
 
+/* 1 if the graph is stored in hub-first ids (chosen at create), 0 if in its
+ * input ids, -1 for a null graph. */
+int32_t dfq_graph_is_hub_first(const dfq_graph* g);
+
+/* The graph's class for tuned-option reuse: "skewed" (stored hub-first) or
+ * "even", then n and the average degree rounded to powers of two, e.g.
+ * "skewed-n2^22-d2^5".  Writes a NUL-terminated string into buf[len] and
+ * returns its length, or a negative status. */
+int dfq_graph_class(const dfq_graph* g, char* buf, int32_t len);
+
+/* dfq_autotune with a persistent cache of tuned options: the JSON file at
+ * cache_path holds one entry per (GPU, graph class), the GPU named by its
+ * device name, SM count and compute capability.  A hit installs the stored
+ * options without timing anything (*hit = 1); a miss tunes and adds the
+ * winner to the file (*hit = 0; the file is rewritten through a temporary
+ * and a rename).  The reference tuned its bins by hand per program and
+ * compared settings offline (design/shared-q/atomic-sa/our-sep/upper-bound/
+ * com-orkut_8-64-1024-16384-all and its siblings). */
+int dfq_autotune_cached(dfq_graph* g, const int32_t* sources, int32_t nsrc, const char* cache_path,
+                        dfq_opts* best, int32_t* hit);
+
 /* ------------------------------------------- graph pools and batched BFS */
 /* No reference counterpart: the reference runs one source per process launch
  * (its '$' mode re-queries one source at a time, DFQ:202-214,302-308).
@@ -293,7 +314,10 @@ int dfq_autotune(dfq_graph* g, const int32_t* sources, int32_t nsrc, dfq_opts* b
  * with at least wide_min_edges edges and average degree >= wide_min_degree)
  * run one after another on the whole grid, then every block pulls "narrow"
  * queries (small or high-diameter graphs) and runs each alone with its block
- * barrier as the level barrier. */
+ * barrier as the level barrier.  Narrow queries on large high-diameter
+ * graphs (>= 65,536 vertices, average degree < 8) run on "gangs" of 2 to 16
+ * blocks from the launch's start when a quarter of the grid leaves at least
+ * two blocks for each of them. */
 typedef struct dfq_pool dfq_pool;
 
 typedef struct dfq_query {
@@ -323,6 +347,19 @@ int dfq_pool_create(const dfq_csr* graphs, int32_t ngraphs, const dfq_opts* opts
 int dfq_pool_destroy(dfq_pool* p);
 int32_t dfq_pool_num_graphs(const dfq_pool* p);
 int dfq_pool_graph_info(const dfq_pool* p, int32_t graph, int32_t* n, int64_t* e, int32_t* wide);
+
+/* The pool's options.  set_opts changes the kernel options of later
+ * launches (a captured batch is re-captured); wide_min_edges,
+ * wide_min_degree and vertex_order are fixed at creation (DFQ_EINVAL). */
+int dfq_pool_get_opts(const dfq_pool* p, dfq_opts* o);
+int dfq_pool_set_opts(dfq_pool* p, const dfq_opts* o);
+
+/* Choose the pool's kernel options by timing dfq_pool_batch on the given
+ * queries (coordinate descent over block size, bin thresholds, piece size,
+ * local queue capacity, probe mode and bulk-copy staging); installs and
+ * returns the winner.  The reference fixed these per program with #defines
+ * (design/shared-q/atomic-sa/our-sep/upper-bound/bfs.cu:16-36). */
+int dfq_pool_autotune(dfq_pool* p, const dfq_query* q, int32_t nq, dfq_opts* best);
 
 /* One query as one plain cooperative launch on the whole grid (synchronous):
  * the per-query baseline batches are compared with. */

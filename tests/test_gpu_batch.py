@@ -89,7 +89,7 @@ def test_batch_with_hot_cache(torch, flags):
     block), with parents: same levels, valid trees."""
     graphs = mixed_graphs()
     o = opts_small_wide()
-    o.hot_cache = 64  # as large as fits beside the layout (with cold rings)
+    o.hot_cache = 32  # 32 KB: the visited bits of the first 262,144 ids
     with d.Pool(graphs, o) as pool:
         qs, meta = make_queries(torch, graphs, 2, seed=5, parents=True)
         res, _ = pool.batch(qs, flags)
@@ -169,3 +169,47 @@ def test_renumbered_wide_graphs(torch):
                 assert np.array_equal(lv, want)
                 assert oracle.validate_tree(g.offsets, g.cols, s, lv, pa) == 0
                 srv.release(rid)
+
+
+def test_pool_autotune_and_set_opts(torch):
+    """The batch kernel tuned on the pool itself: the winner is installed,
+    a captured batch is re-captured after an option change, results stay
+    exact; options fixed at pool creation are refused."""
+    graphs = mixed_graphs()
+    with d.Pool(graphs, opts_small_wide()) as pool:
+        qs, meta = make_queries(torch, graphs, 2, seed=9)
+        res, _ = pool.batch(qs, d.BATCH_GRAPH)
+        check_results(qs, meta, res)
+        best = pool.autotune(qs)
+        assert pool.opts().as_dict() == best.as_dict()
+        res, _ = pool.batch(qs, d.BATCH_GRAPH)
+        check_results(qs, meta, res)
+        o = pool.opts()
+        o.block_threads = 1024 if o.block_threads != 1024 else 512
+        pool.set_opts(o)
+        res, _ = pool.batch(qs, d.BATCH_GRAPH)
+        check_results(qs, meta, res)
+        bad = pool.opts()
+        bad.wide_min_edges = bad.wide_min_edges * 2
+        with pytest.raises(d.DfqError):
+            pool.set_opts(bad)
+
+
+@pytest.mark.parametrize("flags", [0, d.BATCH_GRAPH])
+@pytest.mark.parametrize("parents", [False, True])
+def test_batch_gangs_for_high_diameter_graphs(torch, flags, parents):
+    """Large high-diameter graphs (grids of >= 65,536 vertices) run on gangs
+    of blocks: few such queries get large gangs, many get small ones, and
+    with more queries than gang blocks they fall back to one block each.
+    Every result stays exact, in every mix with wide and narrow queries."""
+    grids = [d.gen_grid(side, 0.02, seed=side)[0] for side in (260, 300, 400)]
+    graphs = grids + [d.gen_rmat(16, 16, seed=5), d.gen_rmat(11, 8, seed=6), d.gen_grid(40, 0.0, seed=1)[0]]
+    o = opts_small_wide()
+    with d.Pool(graphs, o) as pool:
+        for per_graph in (1, 3, 40):  # 3 / 9 / 120 gang queries
+            qs, meta = make_queries(torch, graphs if per_graph < 40 else graphs[:3], per_graph, seed=per_graph,
+                                    parents=parents)
+            res, _ = pool.batch(qs, flags)
+            check_results(qs, meta, res, parents=parents)
+            res, _ = pool.batch(qs, flags)  # a replay of the same shape
+            check_results(qs, meta, res, parents=parents)

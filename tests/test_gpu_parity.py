@@ -180,13 +180,12 @@ def test_level_profile_matches_oracle(kind):
     assert np.all(np.diff(ns) >= 0)
 
 
-@pytest.mark.parametrize("order,hot,block", [(1, 0, 512), (2, 0, 512), (2, -1, 512), (1, 64, 512), (2, 64, 512),
-                                             (2, 8, 512), (2, 64, 1024), (1, 64, 256)])
+@pytest.mark.parametrize("order,hot,block", [(1, 0, 512), (2, 0, 512), (2, -1, 512), (1, 32, 512), (2, 32, 512),
+                                             (2, 8, 512), (2, 32, 1024), (1, 32, 256)])
 def test_vertex_order_and_hot_cache(order, hot, block):
-    """Hub-first relabelling and the shared hot-vertex cache (with the cold
-    rings that batch the probes it cannot settle) change only how the kernel
-    works: levels, parents (in input ids) and E_R stay exact, on the whole
-    grid and in a small graph that the cache covers entirely."""
+    """Hub-first relabelling and the shared hot-vertex cache change only how
+    the kernel works: levels, parents (in input ids) and E_R stay exact, on
+    the whole grid and in a small graph that the cache covers entirely."""
     for g, srcs in [(d.gen_rmat(16, 16, seed=21), None), (d.gen_zipf_geometric(50000, 4.7, 2.1, seed=21), [0, 7])]:
         srcs = srcs or [int(x) for x in g.pick_sources(3, seed=21)]
         with d.Graph(g, opts=opts(vertex_order=order, hot_cache=hot, block_threads=block)) as dg:
@@ -197,8 +196,8 @@ def test_vertex_order_and_hot_cache(order, hot, block):
 
 @pytest.mark.parametrize("block", [256, 512, 1024])
 @pytest.mark.parametrize("tma", [0, 1])
-def test_hot_cache_cold_rings_bin_boundaries(block, tma):
-    """The cold-ring probe path on a hub graph whose degrees sit on every bin
+def test_hot_cache_bin_boundaries(block, tma):
+    """The hot-vertex cache on a hub graph whose degrees sit on every bin
     boundary (small gather, medium warp lists, large pieces), hub-first ids
     forced so the cache holds the hubs: bit-exact levels, valid parents."""
     rng = np.random.default_rng(31)
@@ -211,7 +210,7 @@ def test_hot_cache_cold_rings_bin_boundaries(block, tma):
     src += rng.integers(0, n, m).tolist()
     dst += (rng.zipf(2.0, m) % n).tolist()
     g = d.from_edges(src, dst, n, d.CSR_SYMMETRIZE | d.CSR_DEDUP)
-    with d.Graph(g, opts=opts(hot_cache=64, vertex_order=2, block_threads=block, use_tma=tma)) as dg:
+    with d.Graph(g, opts=opts(hot_cache=32, vertex_order=2, block_threads=block, use_tma=tma)) as dg:
         for s in [0, 7, 15, int(rng.integers(0, n))]:
             run_and_check(g, s, graph=dg)
             run_and_check(g, s, graph=dg, parents=False)
@@ -425,12 +424,12 @@ def test_single_vertex_and_empty_graph():
 
 
 @pytest.mark.parametrize("kw", [{"l2_persist": 1}, {"blocks_per_sm": 1}, {"blocks_per_sm": 2},
-                                {"blocks_per_sm": 1, "block_threads": 1024, "hot_cache": 64},
-                                {"l2_persist": 1, "hot_cache": 64, "vertex_order": 2}])
+                                {"blocks_per_sm": 1, "block_threads": 1024, "hot_cache": 32},
+                                {"l2_persist": 1, "hot_cache": 32, "vertex_order": 2}])
 def test_autotuner_axes_keep_parity(kw):
     """Every option the autotuner can pick runs bit-exact: the L2-persisting
-    bitmap window, capped blocks per SM, and the hot-vertex cache with its
-    cold rings, on a skewed graph (hub-first ids) and a grid."""
+    bitmap window, capped blocks per SM, and the hot-vertex cache, on a
+    skewed graph (hub-first ids) and a grid."""
     rm = d.gen_rmat(17, 16, seed=41)
     grid, _ = d.gen_grid(256, 0.02, seed=41)
     for g, srcs in [(rm, [int(x) for x in rm.pick_sources(3, seed=41)]), (grid, [0, grid.n // 2])]:
@@ -492,3 +491,36 @@ def test_full_size_grid4096_every_source():
     srcs = bench.grid_sources(orig, 4096)
     assert len(srcs) == 16
     _check_all_sources(g, srcs, parents=False)
+
+
+def test_autotune_cache_per_gpu_and_graph_class(tmp_path):
+    """dfq_autotune_cached: a miss tunes and writes a JSON entry keyed by GPU
+    and graph class; a second graph of the same class reuses it without
+    timing; a graph of another class gets its own entry; results stay exact."""
+    import json
+    cache = tmp_path / "tuned.json"
+    g = d.gen_rmat(15, 16, seed=12)
+    srcs = g.pick_sources(2, seed=12)
+    with d.Graph(g) as dg:
+        cls = dg.graph_class()
+        assert cls.startswith("skewed-" if dg.hub_first else "even-") and "-n2^15-" in cls, cls
+        best, hit = dg.autotune_cached(srcs, cache)
+        assert not hit
+        for s in srcs:
+            run_and_check(g, int(s), graph=dg)
+    entries = json.loads(cache.read_text())["entries"]
+    assert len(entries) == 1 and entries[0]["class"] == cls
+    assert entries[0]["opts"]["block_threads"] == best.block_threads
+    h = d.gen_rmat(15, 16, seed=13)
+    with d.Graph(h) as dh:
+        if dh.graph_class() == cls:  # same class: reused without timing
+            again, hit = dh.autotune_cached(h.pick_sources(2, seed=13), cache)
+            assert hit and again.as_dict() == best.as_dict()
+        run_and_check(h, int(h.pick_sources(1, seed=13)[0]), graph=dh)
+    grid, _ = d.gen_grid(128, 0.0, seed=1)
+    with d.Graph(grid) as dgr:
+        assert dgr.graph_class() == "even-n2^14-d2^2"
+        _, hit = dgr.autotune_cached([0, grid.n - 1], cache)
+        assert not hit
+        run_and_check(grid, 0, graph=dgr)
+    assert len(json.loads(cache.read_text())["entries"]) == 2
