@@ -629,6 +629,9 @@ def main():
     ap.add_argument("--no-do", action="store_true", help="skip the direction-optimising line (reported separately)")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of every timed source")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-queries record")
+    ap.add_argument("--ab", action="append", default=[], metavar="NAME=VALUE[,NAME=VALUE]",
+                    help="option A/B: time the default options and each of these variants on the same "
+                         "graph and sources (one JSON line), instead of the benchmark; repeatable")
     ap.add_argument("--opt", action="append", default=[], metavar="NAME=VALUE",
                     help="kernel option for the timed graph (dfq_opts field), e.g. use_tma=0; repeatable")
     args = ap.parse_args()
@@ -655,6 +658,8 @@ def main():
         setattr(o, k, int(v))
     dg = d.Graph(g, opts=o)
     n = g.n
+    if args.ab:
+        return run_ab(args, dg, g, srcs, torch, d, cfg) if rank == 0 else 0
     barrier(pg)
     ck = Clocks(local)
     m = measure_device(dg, srcs, n, args.steps, args.warmup, torch, with_clocks=ck,
@@ -721,7 +726,7 @@ def main():
         # Graph500 counts an undirected edge once: E_R / 2 on a symmetrised graph
         out["graph500_gteps"] = value / 2
     if args.workload == "rmat22" and not args.no_do:
-        out["direction_optimizing"] = direction_optimizing(g, srcs, er, levels, args, torch, d, pg)
+        out["direction_optimizing"] = direction_optimizing(g, srcs, er, rr, levels, args, torch, d, pg)
     if rank == 0 and not args.no_parity:
         # every timed source's levels (from the untimed pass) against the oracle
         out["parity"] = oracle_parity(g.offsets, g.cols, srcs, lambda i: m["host_levels"][i], device_er=er)
@@ -750,7 +755,41 @@ def main():
     return 0
 
 
-def direction_optimizing(g, srcs, er, td_levels, args, torch, d, pg):
+def run_ab(args, dg, g, srcs, torch, d, cfg):
+    """Option A/B on one graph: the graph's options (defaults plus --opt) and
+    each --ab variant, timed like the benchmark (events around every launch,
+    `steps` passes over the sources after `warmup`), each variant's first
+    source checked against the oracle.  One JSON line."""
+    import oracle
+    base = dg.opts()
+    rows = []
+    for spec in [""] + list(args.ab):
+        o = d.Opts.from_buffer_copy(base)
+        for kv in filter(None, spec.split(",")):
+            k, v = kv.split("=", 1)
+            setattr(o, k, int(v))
+        row = {"variant": spec or "base"}
+        try:
+            dg.set_opts(o)
+            m = measure_device(dg, srcs, g.n, args.steps, args.warmup, torch)
+            lv = m["levels_buf"][(len(srcs) - 1) & 1].cpu().numpy()
+            want = oracle.bfs(g.offsets, g.cols, int(srcs[-1]))
+            row.update({"ms_per_bfs_mean": float(np.mean(m["launch_ms"])),
+                        "ms_per_bfs_median": float(np.median(m["launch_ms"])),
+                        "gteps": float(m["er"].sum() * m["launch_ms"].shape[0] / (m["launch_ms"].sum() * 1e-3) / 1e9),
+                        "us_per_level": float(np.median(m["launch_ms"][0] * 1e3 / np.maximum(m["levels"], 1))),
+                        "oracle_mismatches_last_source": int(oracle.compare(want, lv)["mismatches"])})
+        except d.DfqError as e:
+            row["error"] = str(e)
+        rows.append(row)
+    dg.set_opts(base)
+    dg.close()
+    print(json.dumps({"ab": rows, "config": dict(cfg, sources=len(srcs)), "steps": args.steps,
+                      "warmup": args.warmup, "clock": "CUDA events around each launch"}))
+    return 0
+
+
+def direction_optimizing(g, srcs, er, rr, td_levels, args, torch, d, pg):
     """The same sources with direction-optimising levels (dfq_opts.direction = 1,
     Beamer et al. 2012): reported beside the headline, which stays top-down like
     the reference.  GTEPS uses the same E_R per source (the fixed work model),
@@ -765,7 +804,15 @@ def direction_optimizing(g, srcs, er, td_levels, args, torch, d, pg):
     ms = allreduce_max(pg, m["ms_total"])
     steps = m["launch_ms"].shape[0]
     edges = allreduce_sum(pg, float(er.sum() * steps))
+    hbm, peak_kind = peaks()
+    bytes_per_launch = float((4 * er + 8 * rr + 4 * g.n).sum()) / len(srcs)
+    avg_ms = float(np.mean(m["launch_ms"]))
+    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
     return {"value": edges / (ms * 1e-3) / 1e9, "unit": UNIT, "per_bfs_ms_median": float(np.median(m["launch_ms"])),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "peak_kind": peak_kind, "bytes_alg_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
+                         "note": "the same fixed byte model as the headline (4 E_R + 8 |R| + 4 N); a bottom-up "
+                                 "level reads fewer columns than E_R counts"},
             "steps": steps, "levels_match_top_down": same, "bottom_up_levels_last_source": bu_levels,
             "note": "same E_R per source as the headline; levels whose frontier holds > 1/14 of the "
                     "unexplored edges run bottom-up; not the reference's algorithm, so not the headline"}
