@@ -354,6 +354,12 @@ def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 10
                 queries.append((gi, int(s), torch.empty(g.n, dtype=torch.int32, device="cuda")))
         nq = len(queries)
         nwide = sum(1 for q in queries if pool.info(q[0])[2])
+        # query kinds as the batch kernel splits them: wide graphs on the
+        # whole grid, large high-diameter graphs on gangs, the rest on a block
+        kind = []
+        for q in queries:
+            n_, e_, w_ = pool.info(q[0])
+            kind.append("wide" if w_ else "gang" if (n_ >= 65536 and e_ < 8 * n_) else "narrow")
         order = np.random.default_rng(11).permutation(nq)
         # plain launches, one per query (each its own cooperative launch)
         for q in queries[:8]:
@@ -362,8 +368,12 @@ def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 10
         t0 = time.perf_counter()
         plain_ms = [pool.bfs(q[0], q[1], q[2]).kernel_ms for q in queries]
         plain_total_s = time.perf_counter() - t0
+        kinds_all = np.array(kind)
+        pm = np.array(plain_ms)
         plain = {"queries_per_s": nq / plain_total_s, "p50_ms": float(np.percentile(plain_ms, 50)),
-                 "p99_ms": float(np.percentile(plain_ms, 99)), "total_ms": plain_total_s * 1e3}
+                 "p99_ms": float(np.percentile(plain_ms, 99)), "total_ms": plain_total_s * 1e3,
+                 "p99_ms_by_kind": {kd: float(np.percentile(pm[kinds_all == kd], 99))
+                                    for kd in ("wide", "gang", "narrow") if (kinds_all == kd).any()}}
         per_size, edges_all = [], 0
         for bs in sizes:
             groups = [[queries[k] for k in order[i:i + bs]] for i in range(0, nq, bs)]
@@ -386,9 +396,12 @@ def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 10
                 lat.append(lat_step)
             ms = float(np.median(tot_ms))
             lat = np.median(np.array(lat), axis=0)
+            kinds = np.array([kind[k] for k in order])  # queries in the order the batches ran them
             per_size.append({"batch": bs, "launches": len(groups), "cuda_graph": flags != 0,
                              "queries_per_s": nq / (ms * 1e-3),
                              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                             "p99_ms_by_kind": {kd: float(np.percentile(lat[kinds == kd], 99))
+                                                for kd in ("wide", "gang", "narrow") if (kinds == kd).any()},
                              "ms_all": ms})
         # parity: `spot` queries of the last batches against the oracle
         rng = np.random.default_rng(3)
