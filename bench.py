@@ -329,7 +329,17 @@ def pool256_graphs(seed: int = 1, count: int = 256):
     return graphs, specs
 
 
-def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 1024), spot: int = 32) -> dict:
+def kernel_opts(d, args):
+    """Default dfq_opts with the --opt NAME=VALUE overrides applied."""
+    o = d.default_opts()
+    for kv in args.opt:
+        k, v = kv.split("=", 1)
+        setattr(o, k, int(v))
+    return o
+
+
+def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 1024), spot: int = 32,
+                 opts=None) -> dict:
     """The batched configuration: 1024 queries (4 seeded sources per graph) over
     the 256-graph pool, compared with one plain cooperative launch per query
     at matched latency.
@@ -346,7 +356,7 @@ def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 10
     t_gen = time.perf_counter()
     graphs, specs = pool256_graphs()
     t_gen = time.perf_counter() - t_gen
-    pool = d.Pool(graphs, d.default_opts())
+    pool = d.Pool(graphs, opts if opts is not None else d.default_opts())
     try:
         queries = []
         for gi, g in enumerate(graphs):
@@ -430,7 +440,7 @@ def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 10
 def run_batch(args, torch, d):
     """Batched workload line: queries/s of the full 1024-query batch, with the
     matched-latency comparison against per-query plain launches."""
-    rec = batch_record(torch, d, args.steps, args.warmup)
+    rec = batch_record(torch, d, args.steps, args.warmup, opts=kernel_opts(d, args))
     full = rec["batched"][-1]
     out = {"metric": "batched BFS queries/s (1024 queries over 256 graphs)", "value": full["queries_per_s"],
            "unit": "queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": full["ms_all"],
@@ -665,10 +675,7 @@ def main():
     g, all_srcs, cfg = workload_graph(args.workload, args.scale)
     t_gen = time.perf_counter() - t_gen
     srcs = all_srcs[: args.sources]
-    o = d.default_opts()
-    for kv in args.opt:
-        k, v = kv.split("=", 1)
-        setattr(o, k, int(v))
+    o = kernel_opts(d, args)
     dg = d.Graph(g, opts=o)
     n = g.n
     if args.ab:
@@ -762,7 +769,7 @@ def main():
     if rank == 0 and args.workload == "rmat22" and not args.no_secondary:
         out["secondary"] = secondary_grid(torch, d, args)
     if rank == 0 and args.workload == "rmat22" and not args.no_batch:
-        out["batch"] = batch_record(torch, d, min(args.steps, 3), 1)
+        out["batch"] = batch_record(torch, d, min(args.steps, 3), 1, opts=kernel_opts(d, args))
     if rank == 0:
         print(json.dumps(out))
     return 0

@@ -649,18 +649,27 @@ __device__ __forceinline__ void claim4(const Params& p, const Lv& lv, Tally& t, 
             eo[j] = __ldg(p.offsets + v[j] + 1);
         }
     }
+    // all four claim atomics are issued before any result is looked at, so a
+    // lane waits for one atomic round trip, not four in a row (a hub is
+    // claimed on its own word; its winner then sets the hub's bitmap bit for
+    // the probes with a reduction whose result nobody waits for)
+    unsigned old[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        old[j] = 0xffffffffu;
+        if (!(vm >> j & 1)) continue;
+        const bool hub = v[j] < p.hub_n;
+        unsigned* word = hub ? p.hub_claim + v[j] * kHubStride : p.bitmap + (v[j] >> 5);
+        old[j] = atomicOr(word, 1u << (v[j] & 31));
+    }
     unsigned won = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         if (!(vm >> j & 1)) continue;
-        // a hub is claimed on its own word (its winner then sets its bitmap
-        // bit for the probes: one atomic per hub there); others on the bitmap
-        const bool hub = v[j] < p.hub_n;
         const unsigned bit = 1u << (v[j] & 31);
-        unsigned* word = hub ? p.hub_claim + v[j] * kHubStride : p.bitmap + (v[j] >> 5);
-        if (!(atomicOr(word, bit) & bit)) {
+        if (!(old[j] & bit)) {
             won |= 1u << j;
-            if (hub) atomicOr(&p.bitmap[v[j] >> 5], bit);
+            if (v[j] < p.hub_n) atomicOr(&p.bitmap[v[j] >> 5], bit);
         }
         hot_learn(lv, v[j]);  // visited now, whoever won
     }
