@@ -84,6 +84,12 @@ KernelFn pick_kernel(int B, bool par) {
     }
 }
 
+// block_threads = 0: 1024 for graphs of average degree below 8 (grids,
+// meshes: thousands of small levels, where 152 blocks of 32 warps finish a
+// level 5-7 % sooner than 304 blocks of 16, measured on the 4096^2 grid);
+// 512 otherwise (equal on R-MAT, and smaller per-block layouts).
+int auto_block_threads(int32_t n, int64_t e) { return e < 8 * (int64_t)n ? 1024 : 512; }
+
 int validate_opts(const dfq_opts& o) {
     if (o.block_threads != 256 && o.block_threads != 512 && o.block_threads != 1024)
         return fail(DFQ_EINVAL, "block_threads must be 256, 512 or 1024 (got %d)", o.block_threads);
@@ -551,7 +557,7 @@ extern "C" {
 
 void dfq_opts_default(dfq_opts* o) {
     if (!o) return;
-    o->block_threads = 512;
+    o->block_threads = 0;  // chosen per graph at create (auto_block_threads)
     o->blocks_per_sm = 0;
     o->medium_min_degree = 64;
     o->large_min_degree = 256;
@@ -581,7 +587,7 @@ int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int
     dfq_opts o;
     dfq_opts_default(&o);
     if (opts) o = *opts;
-    if (o.block_threads == 0) o.block_threads = 512;
+    if (o.block_threads == 0) o.block_threads = auto_block_threads(n, e);
     if (o.local_queue_cap == 0) o.local_queue_cap = 256;
     if (o.local_edge_budget == 0) o.local_edge_budget = 8192;
     if (o.timeout_ms == 0) o.timeout_ms = 5000;
@@ -679,7 +685,7 @@ int dfq_graph_set_opts(dfq_graph* g, const dfq_opts* o) {
     clear_error();
     if (!g || !o) return fail(DFQ_EINVAL, "dfq_graph_set_opts: null argument");
     dfq_opts v = *o;
-    if (v.block_threads == 0) v.block_threads = 512;
+    if (v.block_threads == 0) v.block_threads = auto_block_threads(g->n, g->e);
     if (v.local_queue_cap == 0) v.local_queue_cap = 256;
     if (v.local_edge_budget == 0) v.local_edge_budget = 8192;
     if (v.timeout_ms == 0) v.timeout_ms = 5000;

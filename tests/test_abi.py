@@ -95,7 +95,7 @@ def test_bad_arguments():
     assert L.dfq_bfs(None, 0, None, None, None) == -1
     assert L.dfq_graph_destroy(None) == -1
     o = d.default_opts()
-    assert o.block_threads in (256, 512, 1024) and o.large_min_degree >= 32
+    assert o.block_threads in (0, 256, 512, 1024) and o.large_min_degree >= 32
     assert d.lib().dfq_graph_num_vertices(None) == -1
 
 
