@@ -655,6 +655,9 @@ def main():
     ap.add_argument("--ab", action="append", default=[], metavar="NAME=VALUE[,NAME=VALUE]",
                     help="option A/B: time the default options and each of these variants on the same "
                          "graph and sources (one JSON line), instead of the benchmark; repeatable")
+    ap.add_argument("--level-profile", type=int, default=None, metavar="FROM",
+                    help="per-level profile of the first source (64 levels from level FROM; with the "
+                         "profiling build loaded through DFQ_LIB also the claim steps), one JSON line")
     ap.add_argument("--opt", action="append", default=[], metavar="NAME=VALUE",
                     help="kernel option for the timed graph (dfq_opts field), e.g. use_tma=0; repeatable")
     args = ap.parse_args()
@@ -680,6 +683,8 @@ def main():
     n = g.n
     if args.ab:
         return run_ab(args, dg, g, srcs, torch, d, cfg) if rank == 0 else 0
+    if args.level_profile is not None:
+        return run_level_profile(args, dg, g, srcs, torch, d, cfg) if rank == 0 else 0
     barrier(pg)
     ck = Clocks(local)
     m = measure_device(dg, srcs, n, args.steps, args.warmup, torch, with_clocks=ck,
@@ -806,6 +811,25 @@ def run_ab(args, dg, g, srcs, torch, d, cfg):
     dg.close()
     print(json.dumps({"ab": rows, "config": dict(cfg, sources=len(srcs)), "steps": args.steps,
                       "warmup": args.warmup, "clock": "CUDA events around each launch"}))
+    return 0
+
+
+def run_level_profile(args, dg, g, srcs, torch, d, cfg):
+    """Per-level profile (dfq_bfs_last_levels with profile on) of the first
+    source after `warmup` runs: frontier, edges, the time to the last block's
+    finish, the spread of block finishes, the barrier, the phase ends and - in
+    the profiling build - the claim steps, for 64 levels from --level-profile."""
+    o = dg.opts()
+    o.profile = max(1, args.level_profile)
+    dg.set_opts(o)
+    lv = torch.empty(g.n, dtype=torch.int32, device="cuda")
+    for _ in range(max(args.warmup, 1) + 1):
+        dg.launch(int(srcs[0]), lv)
+    dg.sync()
+    rows = dg.last_levels(64)
+    print(json.dumps({"level_profile": rows, "source": int(srcs[0]), "config": cfg,
+                      "kernel_opts": dg.opts().as_dict(), "library": os.environ.get("DFQ_LIB", "product build")}))
+    dg.close()
     return 0
 
 

@@ -105,7 +105,7 @@ int validate_opts(const dfq_opts& o) {
     if (o.timeout_ms < 1) return fail(DFQ_EINVAL, "timeout_ms must be >= 1");
     if (o.probe_first < 0 || o.probe_first > 2) return fail(DFQ_EINVAL, "probe_first must be 0, 1 or 2");
     if (o.hot_cache < -1 || o.hot_cache > 32) return fail(DFQ_EINVAL, "hot_cache must be -1, 0 or 1..32 (KB)");
-    if (o.profile != 0 && o.profile != 1) return fail(DFQ_EINVAL, "profile must be 0 or 1");
+    if (o.profile < 0) return fail(DFQ_EINVAL, "profile must be >= 0");
     if (o.direction != 0 && o.direction != 1) return fail(DFQ_EINVAL, "direction must be 0 or 1");
     if (o.stall_test_level < 0) return fail(DFQ_EINVAL, "stall_test_level must be >= 0");
     if (o.vertex_order < 0 || o.vertex_order > 2) return fail(DFQ_EINVAL, "vertex_order must be 0, 1 or 2");
@@ -457,7 +457,8 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
     p.use_tma = o.use_tma;
     p.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     p.hot_words = hot_words;
-    p.profile = o.profile;
+    p.profile = o.profile ? 1 : 0;
+    p.trace_from = (DFQ_CLAIM_PROBES && o.profile > 1) ? o.profile : 0;
     if (o.direction == 1 && !g->symmetric)
         return fail(DFQ_EINVAL, "direction = 1 needs a graph created with direction = 1 (checked undirected)");
     p.direction = o.direction;
@@ -733,7 +734,8 @@ int dfq_bfs_last_trace(dfq_graph* g, int64_t* start_ns, int32_t* frontier, int32
     int rc = fill_stats(g, nullptr, true);
     if (rc) return rc;
     const dfqk::Control& c = *g->ctl_host;
-    int n = std::min(std::min(max_levels, dfqk::kTraceLevels), c.stats.levels + 1);
+    const int from = (DFQ_CLAIM_PROBES && g->opts.profile > 1) ? g->opts.profile : 0;
+    int n = std::min(std::min(max_levels, dfqk::kTraceLevels), std::max(c.stats.levels + 1 - from, 0));
     for (int i = 0; i < n; ++i) {
         start_ns[i] = c.trace_ns[i];
         frontier[i] = c.trace_frontier[i];
@@ -749,10 +751,13 @@ int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels) {
     int rc = fill_stats(g, nullptr, true);
     if (rc) return rc;
     const dfqk::Control& c = *g->ctl_host;
-    int n = std::min(std::min(max_levels, dfqk::kTraceLevels), c.stats.levels + 1);
+    const int from = (DFQ_CLAIM_PROBES && g->opts.profile > 1) ? g->opts.profile : 0;
+    int n = std::min(std::min(max_levels, dfqk::kTraceLevels), std::max(c.stats.levels + 1 - from, 0));
     for (int i = 0; i < n; ++i) {
         dfq_level_info& o = out[i];
         memset(&o, 0, sizeof o);
+        o.level = from + i;
+        for (int k = 0; k < 4; ++k) o.claim_ns[k] = (int32_t)c.trace_claim[i][k];
         o.start_ns = c.trace_ns[i];
         o.frontier = c.trace_frontier[i];
         o.edges = c.trace_edges[i];

@@ -260,9 +260,11 @@ int ensure_blocks(dfq_pool* p, int grid, bool par) {
 // average degree below kGangMaxDegree (a high-diameter graph: a grid, a
 // road-like mesh) runs thousands of levels; on one block each level is slow
 // (a few warps carry its whole frontier), so such queries get a gang of
-// blocks when the batch leaves enough of them: the gang budget is a quarter
-// of the grid, shared evenly (at most kGangMax blocks per gang, at most
-// kGangsMax gangs); with fewer than 2 blocks per query they stay narrow.
+// blocks when the batch leaves enough of them: the gang budget is half the
+// grid, shared evenly (at most kGangMax blocks per gang, at most kGangsMax
+// gangs); with fewer than 2 blocks per query they stay narrow.  Half rather
+// than a quarter measured better on the 256-graph pool: batches of 256 went
+// from 13.4k to 15.7k queries/s with the gang p99 from 19.9 to 16.1 ms.
 constexpr int32_t kGangMinVertices = 1 << 16;
 constexpr int kGangMaxDegree = 8;
 constexpr int kGangMax = 16;
@@ -678,13 +680,13 @@ int dfq_pool_batch(dfq_pool* p, const dfq_query* q, int32_t nq, int32_t flags, d
         else if (gang_graph(p, q[i].graph)) ganged.push_back(i);
         else narrow.push_back(i);
     }
-    // gang size: the gang budget (a quarter of the grid) shared by the gang
-    // queries; below 2 blocks per query they run narrow like the rest
+    // gang size: the gang budget (half the grid) shared by the gang queries;
+    // below 2 blocks per query they run narrow like the rest
     int gang_size = 0, n_gangs = 0;
     if (!ganged.empty()) {
-        gang_size = std::min(kGangMax, (grid / 4) / (int)ganged.size());
+        gang_size = std::min(kGangMax, (grid / 2) / (int)ganged.size());
         if (gang_size >= 2) {
-            n_gangs = std::min<int>({(int)ganged.size(), (grid / 4) / gang_size, kGangsMax});
+            n_gangs = std::min<int>({(int)ganged.size(), (grid / 2) / gang_size, kGangsMax});
         } else {
             narrow.insert(narrow.end(), ganged.begin(), ganged.end());
             ganged.clear();

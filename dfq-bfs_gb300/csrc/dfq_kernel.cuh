@@ -40,6 +40,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// Profiling build only (DFQ_CLAIM_PROBES=1 at build time): with profile on,
+// the claim path records when its steps finish.  0 in the product build, so
+// the probes are not even compiled there.
+#ifndef DFQ_CLAIM_PROBES
+#define DFQ_CLAIM_PROBES 0
+#endif
+
 namespace dfqk {
 
 constexpr unsigned kFull = 0xffffffffu;
@@ -94,6 +101,10 @@ struct Control {
     // with profiling: the latest time (ns after its block's level start) a
     // warp finished the own queue, the pieces, the overflow chunks, the claims
     unsigned trace_phase[kTraceLevels][4];
+    // profiling build: over all warps, the latest time (ns after the warp's
+    // level start) a claim batch had its neighbours in hand, its row bounds
+    // loaded, its claim atomics answered, its pushes done
+    unsigned trace_claim[kTraceLevels][4];
 };
 
 struct Params {
@@ -124,6 +135,7 @@ struct Params {
     // probe levels (0: no cache); a multiple of 32 words, at most kHotWordsMax
     int hot_words;
     int profile;  // 1: record each block's level finish times
+    int trace_from;  // first level of the traced window of kTraceLevels levels
     int direction;  // 1: levels may run bottom-up (undirected graph, checked by the host)
     int e;          // edges (the bottom-up switch compares against the unexplored ones)
     // vertex order: when the graph was relabelled (rank != null) the kernel
@@ -237,6 +249,24 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned
         "%4;" ::"r"(smem_u32(dst)),
         "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
         : "memory");
+}
+
+// First level of the traced window: p.trace_from in the profiling build, 0
+// in the product build (whose level loop then compiles as if untouched).
+#if DFQ_CLAIM_PROBES
+#define DFQ_TRACE_FROM(p) ((p).trace_from)
+#else
+#define DFQ_TRACE_FROM(p) 0
+#endif
+// Slot of level L in the traced window of kTraceLevels levels (out of range: not traced).
+#define DFQ_TSLOT(p, L) ((L) - DFQ_TRACE_FROM(p))
+__device__ __forceinline__ bool in_trace(int t) { return (unsigned)t < (unsigned)kTraceLevels; }
+
+// %globaltimer read after `dep` is available (the input ties the read to it).
+__device__ __forceinline__ unsigned long long globaltimer_after(unsigned dep) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t) : "r"(dep));
+    return t;
 }
 
 // Set when a thread of this block records an error: a one-block group stops
@@ -639,6 +669,15 @@ __device__ __forceinline__ void push_claims(const Params& p, const Lv& lv, unsig
 template <bool PAR>
 __device__ __forceinline__ void claim4(const Params& p, const Lv& lv, Tally& t, const int (&v)[4], unsigned vm,
                                        const int (&par)[4]) {
+    const int slot = DFQ_TSLOT(p, lv.next - 1);  // traced level window
+    const bool probes = DFQ_CLAIM_PROBES && p.profile && (unsigned)slot < (unsigned)kTraceLevels &&
+                        (threadIdx.x & 31) == 0;
+    auto probe_at = [&](int k, unsigned dep) {
+        if (probes)
+            atomicMax(&p.ctl->trace_claim[slot][k],
+                      (unsigned)(globaltimer_after(dep) - sh.level_t0[threadIdx.x >> 5]));
+    };
+    probe_at(0, (unsigned)v[0]);
     int so[4], eo[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -649,6 +688,7 @@ __device__ __forceinline__ void claim4(const Params& p, const Lv& lv, Tally& t, 
             eo[j] = __ldg(p.offsets + v[j] + 1);
         }
     }
+    probe_at(1, (unsigned)(so[0] + eo[0] + so[3] + eo[3]));
     // all four claim atomics are issued before any result is looked at, so a
     // lane waits for one atomic round trip, not four in a row (a hub is
     // claimed on its own word; its winner then sets the hub's bitmap bit for
@@ -693,11 +733,13 @@ __device__ __forceinline__ void claim4(const Params& p, const Lv& lv, Tally& t, 
         if (dg[j] >= p.large_min) lm |= 1u << j;
         else if (dg[j] > 0) loc |= 1u << j;
     }
+    probe_at(2, won | old[0] | old[3]);
     if (won) {
         t.claims += __popc(won);
         sh.claimed = 1;
     }
     push_claims<PAR>(p, lv, loc, lm, st, dg, v);
+    probe_at(3, (unsigned)sh.local_grab);
 }
 
 // Levels that do not probe: claim the scanned neighbours at once.
@@ -1116,9 +1158,10 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
 
     for (; ok; ++L) {
         const int pushed = sh.in[0];
-        if (grank == 0 && tid == 0 && L < kTraceLevels) {
-            ctl->trace_ns[L] = (long long)globaltimer();
-            ctl->trace_frontier[L] = pushed;
+        if (grank == 0 && tid == 0 && in_trace(DFQ_TSLOT(p, L))) {
+            const int TL = DFQ_TSLOT(p, L);
+            ctl->trace_ns[TL] = (long long)globaltimer();
+            ctl->trace_frontier[TL] = pushed;
         }
         if (pushed == 0) break;
         LevelCtr* cin = &ctl->lv[L % 3];
@@ -1187,11 +1230,12 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             for (int i = tid; i < (p.hot_words >> 2); i += B) dst4[i] = __ldcg(src4 + i);
             __syncthreads();
         }
-        if (grank == 0 && tid == 0 && L < kTraceLevels) {
-            ctl->trace_edges[L] = sh.in[4];
-            ctl->trace_ovf[L] = n_ovf;
-            ctl->trace_pieces[L] = total_pieces;
-            ctl->trace_probe[L] = lv.bottom_up ? 2 : lv.probe;
+        if (grank == 0 && tid == 0 && in_trace(DFQ_TSLOT(p, L))) {
+            const int TL = DFQ_TSLOT(p, L);
+            ctl->trace_edges[TL] = sh.in[4];
+            ctl->trace_ovf[TL] = n_ovf;
+            ctl->trace_pieces[TL] = total_pieces;
+            ctl->trace_probe[TL] = lv.bottom_up ? 2 : lv.probe;
         }
         if (lv.bottom_up && grank == 0 && tid == 0) {
             // E_R stays the degree sum of reached vertices: a bottom-up level
@@ -1230,7 +1274,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             //     there are no more pieces than warps each piece goes to one warp;
             //     otherwise the first 3/4 go round-robin and the rest are pulled
             //     from a counter
-                if (p.profile && lane == 0 && L < kTraceLevels)
+                if (p.profile && lane == 0 && in_trace(DFQ_TSLOT(p, L)))
                     atomicMax(&sh.phase_max[0], (unsigned)(globaltimer() - sh.level_t0[warp]));
             // far fewer pieces than warps (a level around a few long lists):
             // each piece is cut into up to 8 ranges, expanded straight from
@@ -1346,7 +1390,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                 }
             }
 
-                if (p.profile && lane == 0 && L < kTraceLevels)
+                if (p.profile && lane == 0 && in_trace(DFQ_TSLOT(p, L)))
                     atomicMax(&sh.phase_max[1], (unsigned)(globaltimer() - sh.level_t0[warp]));
             // (3) global overflow queue in chunks, same schedule as the
             //     pieces; the next chunk index is fetched before the current one
@@ -1386,11 +1430,11 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         }
         // claim whatever candidates this warp still holds
         if (!lv.bottom_up) {
-            if (p.profile && lane == 0 && L < kTraceLevels)
+            if (p.profile && lane == 0 && in_trace(DFQ_TSLOT(p, L)))
                 atomicMax(&sh.phase_max[2], (unsigned)(globaltimer() - sh.level_t0[warp]));
         }
         ring_drain<PAR>(p, lv, t, ring, true);
-        if (p.profile && lane == 0 && L < kTraceLevels)
+        if (p.profile && lane == 0 && in_trace(DFQ_TSLOT(p, L)))
             atomicMax(&sh.phase_max[3], (unsigned)(globaltimer() - sh.level_t0[warp]));
 
         // end of level: publish how much this block pushed, keep its queue
@@ -1425,12 +1469,13 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         cur ^= 1;
         ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in, true,
                            p.stall_level == L + 1 && grank == gsize - 1);
-        if (p.profile && tid == 0 && L < kTraceLevels) {
+        if (p.profile && tid == 0 && in_trace(DFQ_TSLOT(p, L))) {
+            const int TL = DFQ_TSLOT(p, L);
             // recorded after the barrier: its release would otherwise wait for them
-            atomicMax(&ctl->trace_done_last[L], done_ns);
-            atomicMax(&ctl->trace_done_first[L], ~done_ns);
+            atomicMax(&ctl->trace_done_last[TL], done_ns);
+            atomicMax(&ctl->trace_done_first[TL], ~done_ns);
             for (int k = 0; k < 4; ++k) {
-                atomicMax(&ctl->trace_phase[L][k], sh.phase_max[k]);
+                atomicMax(&ctl->trace_phase[TL][k], sh.phase_max[k]);
                 sh.phase_max[k] = 0;
             }
         }

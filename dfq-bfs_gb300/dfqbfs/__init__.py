@@ -19,7 +19,8 @@ from pathlib import Path
 import numpy as np
 
 PKG = Path(__file__).resolve().parent.parent
-LIB_PATH = PKG / "lib" / "libdfq.so"
+# DFQ_LIB names another build of the library (the profiling build of _build.py)
+LIB_PATH = Path(os.environ["DFQ_LIB"]) if os.environ.get("DFQ_LIB") else PKG / "lib" / "libdfq.so"
 
 DFQ_OK = 0
 ERRORS = {
@@ -98,7 +99,8 @@ class ServerResult(C.Structure):
 class LevelInfo(C.Structure):
     _fields_ = [("start_ns", C.c_int64), ("first_done_ns", C.c_int64), ("last_done_ns", C.c_int64),
                 ("frontier", C.c_int32), ("edges", C.c_int32), ("overflow", C.c_int32),
-                ("pieces", C.c_int32), ("probe", C.c_int32), ("pad", C.c_int32), ("phase_ns", C.c_int32 * 4)]
+                ("pieces", C.c_int32), ("probe", C.c_int32), ("level", C.c_int32), ("phase_ns", C.c_int32 * 4),
+                ("claim_ns", C.c_int32 * 4)]
 
 
 class Stats(C.Structure):
@@ -454,8 +456,10 @@ class Graph:
         out = []
         for i in range(k):
             r = buf[i]
-            row = {"frontier": r.frontier, "edges": r.edges, "overflow": r.overflow, "pieces": r.pieces,
-                   "probe": r.probe}
+            row = {"level": r.level, "frontier": r.frontier, "edges": r.edges, "overflow": r.overflow,
+                   "pieces": r.pieces, "probe": r.probe}
+            if any(r.claim_ns):
+                row["us_claim_steps"] = [round(x / 1e3, 2) for x in r.claim_ns]
             if r.last_done_ns:
                 row["us_phases"] = [round(x / 1e3, 2) for x in r.phase_ns]
                 row["us_work"] = (r.last_done_ns - r.start_ns) / 1e3

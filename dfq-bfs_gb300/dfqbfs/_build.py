@@ -44,26 +44,32 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"build step failed ({r.returncode}): {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
 
 
-def build(verbose: bool = False, ptxas_info: bool = False) -> dict:
-    """Compile everything; returns paths of the products."""
-    BUILD.mkdir(exist_ok=True)
-    LIB.mkdir(exist_ok=True)
-    BIN.mkdir(exist_ok=True)
+def build(verbose: bool = False, ptxas_info: bool = False, probes: bool = False) -> dict:
+    """Compile everything; returns paths of the products.  probes=True makes
+    the profiling build instead (claim-step probes compiled in, -DDFQ_CLAIM_PROBES=1)
+    into build_probes/ and lib_probes/; load it with DFQ_LIB=<its libdfq.so>."""
+    build_dir, lib_dir, bin_dir, nvflags = BUILD, LIB, BIN, NVFLAGS
+    if probes:
+        build_dir, lib_dir, bin_dir = PKG / "build_probes", PKG / "lib_probes", PKG / "bin_probes"
+        nvflags = NVFLAGS + ["-DDFQ_CLAIM_PROBES=1"]
+    build_dir.mkdir(exist_ok=True)
+    lib_dir.mkdir(exist_ok=True)
+    bin_dir.mkdir(exist_ok=True)
     hdeps = [INCLUDE / "dfq.h"] + [CSRC / h for h in HEADERS]
     jobs = []
     objs = []
     for s in HOST_SRCS:
-        src, obj = CSRC / s, BUILD / (s + ".o")
+        src, obj = CSRC / s, build_dir / (s + ".o")
         objs.append(obj)
         if _stale(obj, [src] + hdeps):
             jobs.append(["g++", *CXXFLAGS, f"-I{INCLUDE}", f"-I{CUDA_HOME}/include", "-c", str(src), "-o", str(obj)])
     for s in CUDA_SRCS:
-        src, obj = CSRC / s, BUILD / (s + ".o")
+        src, obj = CSRC / s, build_dir / (s + ".o")
         objs.append(obj)
         if _stale(obj, [src] + hdeps) or ptxas_info:
             extra = ["-Xptxas", "-v"] if ptxas_info else []
-            jobs.append([NVCC, *NVFLAGS, *extra, f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
-    main_src, main_obj = CSRC / "bfs_main.cpp", BUILD / "bfs_main.cpp.o"
+            jobs.append([NVCC, *nvflags, *extra, f"-I{INCLUDE}", "-c", str(src), "-o", str(obj)])
+    main_src, main_obj = CSRC / "bfs_main.cpp", build_dir / "bfs_main.cpp.o"
     if _stale(main_obj, [main_src] + hdeps):
         jobs.append(["g++", *CXXFLAGS, f"-I{INCLUDE}", "-c", str(main_src), "-o", str(main_obj)])
     logs = []
@@ -77,12 +83,12 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict:
             raise RuntimeError(f"build step failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         if r.stderr.strip():
             logs.append(r.stderr)
-    lib = LIB / "libdfq.so"
+    lib = lib_dir / "libdfq.so"
     if _stale(lib, objs):
         _run([NVCC, *ARCH, "-shared", "-cudart", "shared", *map(str, objs), "-o", str(lib), "-lpthread"])
-    exe = BIN / "bfs"
+    exe = bin_dir / "bfs"
     if _stale(exe, [main_obj, lib]):
-        _run(["g++", str(main_obj), "-o", str(exe), f"-L{LIB}", "-ldfq", f"-Wl,-rpath,$ORIGIN/../lib",
+        _run(["g++", str(main_obj), "-o", str(exe), f"-L{lib_dir}", "-ldfq", f"-Wl,-rpath,$ORIGIN/../lib",
               f"-L{CUDA_HOME}/lib64", f"-Wl,-rpath,{CUDA_HOME}/lib64", "-lcudart", "-lpthread"])
     if verbose and logs:
         print("\n".join(logs))
@@ -91,6 +97,6 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> dict:
 
 if __name__ == "__main__":
     import sys
-    out = build(verbose=True, ptxas_info="--ptxas" in sys.argv)
+    out = build(verbose=True, ptxas_info="--ptxas" in sys.argv, probes="--probes" in sys.argv)
     print(out["log"])
     print(out["lib"], out["bin"])

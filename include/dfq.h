@@ -159,7 +159,9 @@ typedef struct dfq_opts {
                                    input ids, 2 = hub-first always.  Results are always reported
                                    in the input ids. */
     int32_t profile;            /* 1: also record when each block finished each level (the
-                                   spread and barrier times of dfq_bfs_last_levels) */
+                                   spread and barrier times of dfq_bfs_last_levels); k > 1 in the
+                                   profiling build (DFQ_CLAIM_PROBES=1): the same, for the 64
+                                   levels from level k on (the product build traces levels 0-63) */
     int32_t direction;          /* 0: top-down levels only (the reference's algorithm);
                                    1: direction-optimising - levels whose frontier holds many
                                    edges run bottom-up (each unvisited vertex looks for a parent
@@ -257,10 +259,15 @@ typedef struct dfq_level_info {
     int32_t overflow;       /* entries read from the global overflow queue */
     int32_t pieces;         /* large-list pieces */
     int32_t probe;          /* 1: probe-then-claim level, 0: claim at once, 2: bottom-up */
-    int32_t pad;
+    int32_t level;          /* the level's index (the traced window starts at level 0, or in
+                               the profiling build at dfq_opts.profile when that is > 1) */
     /* with profile: over all warps, the latest time (ns after the warp began the level) a warp
      * finished its block's own queue, the large-list pieces, the overflow queue, and its claims */
     int32_t phase_ns[4];
+    /* profiling build only (library built with DFQ_CLAIM_PROBES=1), with profile: the latest
+     * time (ns after the warp began the level) a claim batch had its neighbours in hand, had
+     * their row bounds, had its claim atomics answered, and had pushed its winners; else 0 */
+    int32_t claim_ns[4];
 } dfq_level_info;
 int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels);
 
@@ -319,8 +326,8 @@ int dfq_autotune_cached(dfq_graph* g, const int32_t* sources, int32_t nsrc, cons
  * queries (small or high-diameter graphs) and runs each alone with its block
  * barrier as the level barrier.  Narrow queries on large high-diameter
  * graphs (>= 65,536 vertices, average degree < 8) run on "gangs" of 2 to 16
- * blocks from the launch's start when a quarter of the grid leaves at least
- * two blocks for each of them. */
+ * blocks from the launch's start when half the grid leaves at least two
+ * blocks for each of them. */
 typedef struct dfq_pool dfq_pool;
 
 typedef struct dfq_query {
