@@ -88,7 +88,14 @@ KernelFn pick_kernel(int B, bool par) {
 // meshes: thousands of small levels, where 152 blocks of 32 warps finish a
 // level 5-7 % sooner than 304 blocks of 16, measured on the 4096^2 grid);
 // 512 otherwise (equal on R-MAT, and smaller per-block layouts).
-int auto_block_threads(int32_t n, int64_t e) { return e < 8 * (int64_t)n ? 1024 : 512; }
+// The larger blocks only where their shared-memory layout (with parents and
+// the requested hot cache) fits; else 512.
+int auto_block_threads(int32_t n, int64_t e, const dfq_opts& o) {
+    if (e >= 8 * (int64_t)n) return 512;
+    const dfqk::SmemLayout L = dfqk::smem_layout(1024, o.local_queue_cap ? o.local_queue_cap : 256, o.piece_edges, true);
+    const int need = L.bytes + (o.hot_cache > 0 ? 4 * dfqk::kHotWordsMax : 0);
+    return need <= 227 * 1024 ? 1024 : 512;
+}
 
 int validate_opts(const dfq_opts& o) {
     if (o.block_threads != 256 && o.block_threads != 512 && o.block_threads != 1024)
@@ -588,7 +595,7 @@ int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int
     dfq_opts o;
     dfq_opts_default(&o);
     if (opts) o = *opts;
-    if (o.block_threads == 0) o.block_threads = auto_block_threads(n, e);
+    if (o.block_threads == 0) o.block_threads = auto_block_threads(n, e, o);
     if (o.local_queue_cap == 0) o.local_queue_cap = 256;
     if (o.local_edge_budget == 0) o.local_edge_budget = 8192;
     if (o.timeout_ms == 0) o.timeout_ms = 5000;
@@ -686,7 +693,7 @@ int dfq_graph_set_opts(dfq_graph* g, const dfq_opts* o) {
     clear_error();
     if (!g || !o) return fail(DFQ_EINVAL, "dfq_graph_set_opts: null argument");
     dfq_opts v = *o;
-    if (v.block_threads == 0) v.block_threads = auto_block_threads(g->n, g->e);
+    if (v.block_threads == 0) v.block_threads = auto_block_threads(g->n, g->e, v);
     if (v.local_queue_cap == 0) v.local_queue_cap = 256;
     if (v.local_edge_budget == 0) v.local_edge_budget = 8192;
     if (v.timeout_ms == 0) v.timeout_ms = 5000;
