@@ -339,7 +339,7 @@ def kernel_opts(d, args):
 
 
 def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 1024), spot: int = 32,
-                 opts=None) -> dict:
+                 opts=None, tune: bool = False) -> dict:
     """The batched configuration: 1024 queries (4 seeded sources per graph) over
     the 256-graph pool, compared with one plain cooperative launch per query
     at matched latency.
@@ -363,6 +363,16 @@ def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 10
             for s in g.pick_sources(4, seed=gi):
                 queries.append((gi, int(s), torch.empty(g.n, dtype=torch.int32, device="cuda")))
         nq = len(queries)
+        tuned = None
+        if tune:  # dfq_pool_autotune on the full batch, then everything below runs tuned
+            base_opts = pool.opts().as_dict()
+            for _ in range(2):
+                pool.batch(queries, 0)
+            t0 = time.perf_counter()
+            _, ms0 = pool.batch(queries, 0)
+            best = pool.autotune(queries)
+            tuned = {"default_opts": base_opts, "tuned_opts": best.as_dict(),
+                     "tune_s": round(time.perf_counter() - t0, 1), "full_batch_ms_default": ms0}
         nwide = sum(1 for q in queries if pool.info(q[0])[2])
         # query kinds as the batch kernel splits them: wide graphs on the
         # whole grid, large high-diameter graphs on gangs, the rest on a block
@@ -425,7 +435,8 @@ def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 10
         return {"workload": "batch_256graphs_1024q", "graphs": len(graphs),
                 "rmat": sum(1 for sp in specs if sp[0] == "rmat"), "grids": sum(1 for sp in specs if sp[0] == "grid"),
                 "queries": nq, "wide_queries": nwide, "total_edges": int(sum(g.e for g in graphs)),
-                "gen_s": round(t_gen, 1), "per_query_plain": plain, "batched": per_size,
+                "gen_s": round(t_gen, 1), "per_query_plain": plain, "batched": per_size, "autotune": tuned,
+                "kernel_opts": pool.opts().as_dict(),
                 "speedup_qps_full_batch": full["queries_per_s"] / plain["queries_per_s"],
                 "at_equal_p99": ({"batch": eq["batch"], "queries_per_s": eq["queries_per_s"], "p99_ms": eq["p99_ms"],
                                   "speedup_qps": eq["queries_per_s"] / plain["queries_per_s"]} if eq else None),
@@ -440,7 +451,7 @@ def batch_record(torch, d, steps: int, warmup: int, sizes=(64, 128, 256, 512, 10
 def run_batch(args, torch, d):
     """Batched workload line: queries/s of the full 1024-query batch, with the
     matched-latency comparison against per-query plain launches."""
-    rec = batch_record(torch, d, args.steps, args.warmup, opts=kernel_opts(d, args))
+    rec = batch_record(torch, d, args.steps, args.warmup, opts=kernel_opts(d, args), tune=args.pool_autotune)
     full = rec["batched"][-1]
     out = {"metric": "batched BFS queries/s (1024 queries over 256 graphs)", "value": full["queries_per_s"],
            "unit": "queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": full["ms_all"],
@@ -655,6 +666,8 @@ def main():
     ap.add_argument("--ab", action="append", default=[], metavar="NAME=VALUE[,NAME=VALUE]",
                     help="option A/B: time the default options and each of these variants on the same "
                          "graph and sources (one JSON line), instead of the benchmark; repeatable")
+    ap.add_argument("--pool-autotune", action="store_true",
+                    help="batch workload: tune the batch kernel on the pool (dfq_pool_autotune) first")
     ap.add_argument("--level-profile", type=int, default=None, metavar="FROM",
                     help="per-level profile of the first source (64 levels from level FROM; with the "
                          "profiling build loaded through DFQ_LIB also the claim steps), one JSON line")
@@ -790,10 +803,17 @@ def run_ab(args, dg, g, srcs, torch, d, cfg):
     rows = []
     for spec in [""] + list(args.ab):
         o = d.Opts.from_buffer_copy(base)
-        for kv in filter(None, spec.split(",")):
-            k, v = kv.split("=", 1)
-            setattr(o, k, int(v))
         row = {"variant": spec or "base"}
+        if spec == "autotune":  # dfq_autotune on the first 8 sources, from the defaults
+            dg.set_opts(base)
+            t0 = time.perf_counter()
+            o = dg.autotune(srcs[:8])
+            row["tune_s"] = round(time.perf_counter() - t0, 1)
+            row["opts"] = o.as_dict()
+        else:
+            for kv in filter(None, spec.split(",")):
+                k, v = kv.split("=", 1)
+                setattr(o, k, int(v))
         try:
             dg.set_opts(o)
             m = measure_device(dg, srcs, g.n, args.steps, args.warmup, torch)
