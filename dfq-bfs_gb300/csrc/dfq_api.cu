@@ -765,6 +765,7 @@ int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels) {
         memset(&o, 0, sizeof o);
         o.level = from + i;
         for (int k = 0; k < 4; ++k) o.claim_ns[k] = (int32_t)c.trace_claim[i][k];
+        for (int k = 0; k < 4; ++k) o.piece_stats[k] = (int64_t)c.trace_piece[i][k];
         o.start_ns = c.trace_ns[i];
         o.frontier = c.trace_frontier[i];
         o.edges = c.trace_edges[i];

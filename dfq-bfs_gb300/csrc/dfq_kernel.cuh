@@ -105,6 +105,10 @@ struct Control {
     // level start) a claim batch had its neighbours in hand, its row bounds
     // loaded, its claim atomics answered, its pushes done
     unsigned trace_claim[kTraceLevels][4];
+    // profiling build: sums over all warps of the staged-piece path - pieces
+    // expanded, ns waiting for their bulk copies, ns expanding them (claims
+    // included) - and ns spent in candidate claim drains on any path
+    unsigned long long trace_piece[kTraceLevels][4];
 };
 
 struct Params {
@@ -758,6 +762,10 @@ __device__ __forceinline__ void visit4(const Params& p, const Lv& lv, Tally& t, 
 template <bool PAR>
 __device__ __forceinline__ void ring_drain(const Params& p, const Lv& lv, Tally& t, Ring& r, bool all) {
     const int lane = threadIdx.x & 31;
+    const int dslot = DFQ_TSLOT(p, lv.next - 1);
+    const bool dprobe = DFQ_CLAIM_PROBES && p.profile && in_trace(dslot) && lane == 0 &&
+                        (r.n >= 128 || (all && r.n > 0));
+    const unsigned long long d0 = dprobe ? globaltimer() : 0ull;
     while (r.n >= 128 || (all && r.n > 0)) {
         const int take = r.n < 128 ? r.n : 128;
         int v[4], par[4];
@@ -779,6 +787,7 @@ __device__ __forceinline__ void ring_drain(const Params& p, const Lv& lv, Tally&
         r.n -= take;
         claim4<PAR>(p, lv, t, v, vm, par);
     }
+    if (dprobe) atomicAdd(&p.ctl->trace_piece[dslot][3], globaltimer_after(t.claims) - d0);
 }
 
 // Probe levels: test up to four neighbours per lane against the visited
@@ -1348,7 +1357,9 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                         gn = grab();
                     }
                     if (p.use_tma) {
+                        const unsigned long long pw0 = DFQ_CLAIM_PROBES && p.profile ? globaltimer() : 0ull;
                         const bool landed = mbar_wait_bounded(&wbar[cb], (phase_bits >> cb) & 1u, p.timeout_ns);
+                        const unsigned long long pw1 = DFQ_CLAIM_PROBES && p.profile ? globaltimer() : 0ull;
                         if (__any_sync(kFull, !landed)) {
                             // never expand a buffer whose copy did not land: record the
                             // error, give this warp's copies one more bounded wait, stop
@@ -1366,6 +1377,12 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                         const int a0 = lo & ~3, off = lo - a0, tw = hi - a0;
                         if (lv.probe) {
                             probe_piece<PAR>(p, lv, t, ring, buf, off, tw, par0);
+                            if (DFQ_CLAIM_PROBES && p.profile && lane == 0 && in_trace(DFQ_TSLOT(p, L))) {
+                                const int ps = DFQ_TSLOT(p, L);
+                                atomicAdd(&ctl->trace_piece[ps][0], 1ull);
+                                atomicAdd(&ctl->trace_piece[ps][1], pw1 - pw0);
+                                atomicAdd(&ctl->trace_piece[ps][2], globaltimer_after(t.edges) - pw1);
+                            }
                         } else {
                             const int par[4] = {par0, par0, par0, par0};
                             for (int base = 0; base < tw; base += 128) {

@@ -100,7 +100,7 @@ class LevelInfo(C.Structure):
     _fields_ = [("start_ns", C.c_int64), ("first_done_ns", C.c_int64), ("last_done_ns", C.c_int64),
                 ("frontier", C.c_int32), ("edges", C.c_int32), ("overflow", C.c_int32),
                 ("pieces", C.c_int32), ("probe", C.c_int32), ("level", C.c_int32), ("phase_ns", C.c_int32 * 4),
-                ("claim_ns", C.c_int32 * 4)]
+                ("claim_ns", C.c_int32 * 4), ("piece_stats", C.c_int64 * 4)]
 
 
 class Stats(C.Structure):
@@ -460,6 +460,12 @@ class Graph:
                    "pieces": r.pieces, "probe": r.probe}
             if any(r.claim_ns):
                 row["us_claim_steps"] = [round(x / 1e3, 2) for x in r.claim_ns]
+            if any(r.piece_stats):
+                np_ = max(r.piece_stats[0], 1)
+                row["pieces_staged"] = r.piece_stats[0]
+                row["us_per_piece_wait_expand"] = [round(r.piece_stats[1] / np_ / 1e3, 3),
+                                                   round(r.piece_stats[2] / np_ / 1e3, 3)]
+                row["ms_claim_drains_all_warps"] = round(r.piece_stats[3] / 1e6, 3)
             if r.last_done_ns:
                 row["us_phases"] = [round(x / 1e3, 2) for x in r.phase_ns]
                 row["us_work"] = (r.last_done_ns - r.start_ns) / 1e3

@@ -268,6 +268,10 @@ typedef struct dfq_level_info {
      * time (ns after the warp began the level) a claim batch had its neighbours in hand, had
      * their row bounds, had its claim atomics answered, and had pushed its winners; else 0 */
     int32_t claim_ns[4];
+    /* profiling build only, with profile: sums over all warps of the staged large-list pieces
+     * expanded on a probe level, the ns spent waiting for their bulk copies, the ns spent
+     * expanding them (claims included), and the ns spent in candidate claim drains anywhere */
+    int64_t piece_stats[4];
 } dfq_level_info;
 int dfq_bfs_last_levels(dfq_graph* g, dfq_level_info* out, int32_t max_levels);
 
