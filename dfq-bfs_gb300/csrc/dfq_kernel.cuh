@@ -448,9 +448,23 @@ struct BlockShared {
     int hot_off;                    // byte offset of the hot-vertex cache in dynamic shared memory
     unsigned long long level_t0[32];  // profiling: when each warp started the level
     unsigned phase_max[4];            // profiling: this block's latest warp phase ends
+#if DFQ_CLAIM_PROBES
+    unsigned long long acc[32][4];    // profiling build: per-warp sums for trace_piece, flushed per level
+    unsigned claim_max[4];            // profiling build: this block's latest claim steps, flushed per level
+#endif
 };
 static __shared__ BlockShared sh;
 extern __shared__ __align__(128) unsigned char dfq_smem[];
+
+// Profiling build: add v to this warp's accumulator k (lane 0 calls it).
+__device__ __forceinline__ void acc_add(int k, unsigned long long v) {
+#if DFQ_CLAIM_PROBES
+    sh.acc[threadIdx.x >> 5][k] += v;
+#else
+    (void)k;
+    (void)v;
+#endif
+}
 
 // Uniform per-level values.
 struct Lv {
@@ -677,9 +691,13 @@ __device__ __forceinline__ void claim4(const Params& p, const Lv& lv, Tally& t, 
     const bool probes = DFQ_CLAIM_PROBES && p.profile && (unsigned)slot < (unsigned)kTraceLevels &&
                         (threadIdx.x & 31) == 0;
     auto probe_at = [&](int k, unsigned dep) {
+#if DFQ_CLAIM_PROBES
         if (probes)
-            atomicMax(&p.ctl->trace_claim[slot][k],
-                      (unsigned)(globaltimer_after(dep) - sh.level_t0[threadIdx.x >> 5]));
+            atomicMax(&sh.claim_max[k], (unsigned)(globaltimer_after(dep) - sh.level_t0[threadIdx.x >> 5]));
+#else
+        (void)k;
+        (void)dep;
+#endif
     };
     probe_at(0, (unsigned)v[0]);
     int so[4], eo[4];
@@ -787,7 +805,7 @@ __device__ __forceinline__ void ring_drain(const Params& p, const Lv& lv, Tally&
         r.n -= take;
         claim4<PAR>(p, lv, t, v, vm, par);
     }
-    if (dprobe) atomicAdd(&p.ctl->trace_piece[dslot][3], globaltimer_after(t.claims) - d0);
+    if (dprobe) acc_add(3, globaltimer_after(t.claims) - d0);
 }
 
 // Probe levels: test up to four neighbours per lane against the visited
@@ -1147,6 +1165,11 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         s_block_err = 0;
         sh.hot_off = lay.hot_off;
         for (int k = 0; k < 4; ++k) sh.phase_max[k] = 0;
+#if DFQ_CLAIM_PROBES
+        for (int w = 0; w < 32; ++w)
+            for (int k = 0; k < 4; ++k) sh.acc[w][k] = 0ull;
+        for (int k = 0; k < 4; ++k) sh.claim_max[k] = 0;
+#endif
         sh.local_pack = 0ull;
         sh.cnt_cur = sh.local_grab = sh.ovf_pushed = sh.large_pushed = sh.large_pieces = sh.claimed = 0;
         sh.ovf_edges = sh.large_edges = 0;
@@ -1378,10 +1401,9 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                         if (lv.probe) {
                             probe_piece<PAR>(p, lv, t, ring, buf, off, tw, par0);
                             if (DFQ_CLAIM_PROBES && p.profile && lane == 0 && in_trace(DFQ_TSLOT(p, L))) {
-                                const int ps = DFQ_TSLOT(p, L);
-                                atomicAdd(&ctl->trace_piece[ps][0], 1ull);
-                                atomicAdd(&ctl->trace_piece[ps][1], pw1 - pw0);
-                                atomicAdd(&ctl->trace_piece[ps][2], globaltimer_after(t.edges) - pw1);
+                                acc_add(0, 1ull);
+                                acc_add(1, pw1 - pw0);
+                                acc_add(2, globaltimer_after(t.edges) - pw1);
                             }
                         } else {
                             const int par[4] = {par0, par0, par0, par0};
@@ -1454,6 +1476,14 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         if (p.profile && lane == 0 && in_trace(DFQ_TSLOT(p, L)))
             atomicMax(&sh.phase_max[3], (unsigned)(globaltimer() - sh.level_t0[warp]));
 
+#if DFQ_CLAIM_PROBES
+        if (p.profile && lane == 0) {
+            if (in_trace(DFQ_TSLOT(p, L)))
+                for (int k = 0; k < 4; ++k)
+                    if (sh.acc[warp][k]) atomicAdd(&ctl->trace_piece[DFQ_TSLOT(p, L)][k], sh.acc[warp][k]);
+            for (int k = 0; k < 4; ++k) sh.acc[warp][k] = 0ull;
+        }
+#endif
         // end of level: publish how much this block pushed, keep its queue
         __syncthreads();
         unsigned long long done_ns = 0;  // when this block finished the level (thread 0, profiling)
@@ -1491,6 +1521,12 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             // recorded after the barrier: its release would otherwise wait for them
             atomicMax(&ctl->trace_done_last[TL], done_ns);
             atomicMax(&ctl->trace_done_first[TL], ~done_ns);
+#if DFQ_CLAIM_PROBES
+            for (int k = 0; k < 4; ++k) {
+                atomicMax(&ctl->trace_claim[TL][k], sh.claim_max[k]);
+                sh.claim_max[k] = 0;
+            }
+#endif
             for (int k = 0; k < 4; ++k) {
                 atomicMax(&ctl->trace_phase[TL][k], sh.phase_max[k]);
                 sh.phase_max[k] = 0;
