@@ -1335,11 +1335,23 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                 // dependent load or atomic sits between two pieces.  The next
                 // static index lives in the warp's gather scratch (unused while
                 // pieces are expanded).
+                // The dynamic tail is handed out in runs of g_run pieces per atomic:
+                // one counter serves every warp of the grid, and on a level of
+                // ~10^5 tail pieces one atomic per piece queued behind each other
+                // at that counter's L2 slice.  pq[1], pq[2]: this warp's run.
+                const int g_run = max(1, (total_pieces - p_static) / (4 * nwarps));
                 int* pq = wl;
                 auto grab = [&]() -> int {  // lane 0: next piece index (total_pieces: none)
                     const int sn = pq[0];
                     if (sn < p_static) { pq[0] = sn + nwarps; return sn; }
-                    if (p_static < total_pieces) return p_static + atomicAdd(&cin->large_grab, 1);
+                    if (p_static < total_pieces) {
+                        if (pq[1] < pq[2]) return pq[1]++;
+                        const int b = p_static + atomicAdd(&cin->large_grab, g_run);
+                        if (b >= total_pieces) return total_pieces;
+                        pq[1] = b + 1;
+                        pq[2] = min(b + g_run, total_pieces);
+                        return b;
+                    }
                     return total_pieces;
                 };
                 auto desc = [&](int g, int2& d, int& u) {  // lane 0: piece g's range (empty: none)
@@ -1362,6 +1374,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                 int uc = 0, un = 0, gn = total_pieces;
                 if (lane == 0) {
                     pq[0] = gwarp;
+                    pq[1] = pq[2] = 0;
                     desc(grab(), dc, uc);
                     issue(dc, 0);
                     desc(grab(), dn, un);
@@ -1442,10 +1455,27 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                 const int csz = fine ? min(32, max(1, (n_ovf + nwarps - 1) / nwarps)) : 32;
                 const int n_chunks = (n_ovf + csz - 1) / csz;
                 const int c_static = n_chunks <= nwarps ? n_chunks : n_chunks - (n_chunks >> 2);
-                int s_next = gwarp;
+                // The dynamic tail goes out in runs of g_run chunks per atomic, as
+                // for pieces.  g_run is a power of two and run k is chunks
+                // c_static + [k*g_run, (k+1)*g_run), so one register holds the
+                // warp's position: the next static chunk, then the next chunk of
+                // its run, and n_chunks when it must take a new run.
+                const int g_run = 1 << (31 - __clz(max(1, (n_chunks - c_static) / (4 * nwarps))));
+                int s_next = gwarp < c_static ? gwarp : n_chunks;
                 auto next_chunk = [&]() -> int {  // lane 0 only
-                    if (s_next < c_static) { const int ci = s_next; s_next += nwarps; return ci; }
-                    if (c_static < n_chunks) return c_static + atomicAdd(&cin->ovf_grab, 1);
+                    if (s_next < c_static) {
+                        const int ci = s_next;
+                        s_next += nwarps;
+                        if (s_next >= c_static) s_next = n_chunks;
+                        return ci;
+                    }
+                    if (c_static < n_chunks) {
+                        if (s_next < n_chunks && ((s_next - c_static) & (g_run - 1))) return s_next++;
+                        const int b = c_static + atomicAdd(&cin->ovf_grab, g_run);
+                        if (b >= n_chunks) return n_chunks;
+                        s_next = b + 1;
+                        return b;
+                    }
                     return n_chunks;
                 };
                 int nxt = 0;
