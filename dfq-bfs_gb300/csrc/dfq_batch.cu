@@ -150,36 +150,36 @@ template <int B, bool PAR>
 __global__ void __launch_bounds__(B, 1024 / B) dfq_batch_kernel(const __grid_constant__ BatchParams bp) {
     __shared__ Params sp;
     __shared__ int s_q, s_gsize, s_grank;
+    // thread 0's schedule state lives in shared memory and the block's shape
+    // (wide / gang, rank) is recomputed from the launch parameters per round,
+    // so no register stays live across bfs_run beyond the warp state
+    __shared__ unsigned s_round;  // gang rounds taken (0: this block is in no gang or left it)
+    __shared__ int s_k;           // next wide query of this block
     init_warp_barriers<B, PAR>(bp.local_cap, bp.piece_edges);
     WarpState ws{0u, false};
-    if (blockIdx.x == 0 && threadIdx.x == 0) *bp.t0 = (long long)globaltimer();
-    // the last `reserve` blocks skip the wide queries: first the gangs, then
+    if (threadIdx.x == 0) {
+        if (blockIdx.x == 0) *bp.t0 = (long long)globaltimer();
+        const int gang_rel = (int)blockIdx.x - ((int)gridDim.x - bp.n_gangs * bp.gang_size);
+        s_round = bp.n_gangs > 0 && gang_rel >= 0 ? 1u : 0u;
+        s_k = (int)blockIdx.x < (int)gridDim.x - bp.reserve ? 0 : bp.n_wide;
+    }
+    // The last `reserve` blocks skip the wide queries: first the gangs, then
     // blocks that start on the narrow ones (costliest first) at once, so the
     // longest narrow runs overlap the wide phase instead of trailing it; the
-    // wide queries run on the others
-    const int wide_blocks = (int)gridDim.x - bp.reserve;
-    const bool in_wide = (int)blockIdx.x < wide_blocks;
-    const int gang_rel = (int)blockIdx.x - ((int)gridDim.x - bp.n_gangs * bp.gang_size);
-    int gang = -1, gang_rank = 0;  // this block's gang and its rank there (-1: none)
-    if (bp.n_gangs > 0 && gang_rel >= 0) {
-        gang = gang_rel / bp.gang_size;
-        gang_rank = gang_rel % bp.gang_size;
-    }
+    // wide queries run on the others.
     // Gang phase first (gang blocks): the gang's first block takes the next
     // gang query and publishes it; every member waits for the publication
     // (bounded), then the gang runs the query with its blocks as the group.
     // A member reads a round's word before that run's first group barrier,
     // and the first block publishes the next round only after the run, so no
     // round is missed.  Then wide queries (wide blocks), then narrow pulls.
-    // Only thread 0 keeps the schedule state.
-    bool gang_phase = gang >= 0;
-    unsigned round = 0;
-    int k = in_wide ? 0 : bp.n_wide;
     for (;;) {
         if (threadIdx.x == 0) {
             s_q = -1;
-            if (gang_phase) {
-                ++round;
+            if (s_round) {
+                const int gang_rel = (int)blockIdx.x - ((int)gridDim.x - bp.n_gangs * bp.gang_size);
+                const int gang = gang_rel / bp.gang_size, gang_rank = gang_rel % bp.gang_size;
+                const unsigned round = s_round;
                 unsigned long long* word = bp.gang_word + gang;
                 if (gang_rank == 0) {
                     const int j = atomicAdd(bp.gang_next, 1);
@@ -197,16 +197,17 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_batch_kernel(const __grid_con
                     s_q = q;
                     s_gsize = bp.gang_size;
                     s_grank = gang_rank;
+                    s_round = round + 1;
                     fill_params(sp, bp, q, gang_workspace(bp, gang));
                     if (gang_rank == 0) bp.queries[q].t_start = (long long)globaltimer();
                 } else {
-                    gang_phase = false;
+                    s_round = 0;
                 }
             }
-            if (!gang_phase && s_q < 0) {
-                if (k < bp.n_wide) {
-                    s_q = bp.wide_list[k++];
-                    s_gsize = wide_blocks;
+            if (s_q < 0) {
+                if (s_k < bp.n_wide) {
+                    s_q = bp.wide_list[s_k++];
+                    s_gsize = (int)gridDim.x - bp.reserve;
                     s_grank = (int)blockIdx.x;
                     fill_params(sp, bp, s_q, bp.wide_ws);
                     if (blockIdx.x == 0) bp.queries[s_q].t_start = (long long)globaltimer();
@@ -223,11 +224,10 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_batch_kernel(const __grid_con
             }
         }
         __syncthreads();
-        const int qi = s_q;
-        if (qi < 0) break;
+        if (s_q < 0) break;
         bfs_run<B, PAR>(sp, s_gsize, s_grank, ws);
         // the group's first block records the end (block 0 for wide queries)
-        if (threadIdx.x == 0 && s_grank == 0) bp.queries[qi].t_end = (long long)globaltimer();
+        if (threadIdx.x == 0 && s_grank == 0) bp.queries[s_q].t_end = (long long)globaltimer();
         __syncthreads();
     }
 }
