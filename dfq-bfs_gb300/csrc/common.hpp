@@ -80,6 +80,11 @@ int check_opts(const dfq_opts& o);
 // that runs one BFS on a whole cooperative grid; null for an unsupported size.
 const void* single_source_kernel(int block_threads, bool par);
 
+// The cluster form dfqk::dfq_cluster_kernel<block_threads, par> (compiled in
+// dfq_cluster.cu): one thread-block cluster runs the BFS; null for a block
+// size it is not built for (512 and 1024 only).
+const void* cluster_kernel(int block_threads, bool par);
+
 // Run body(i) for i in [0, t) on t threads (the caller's thread takes i = 0).
 template <class F>
 void run_threads(int t, F&& body) {

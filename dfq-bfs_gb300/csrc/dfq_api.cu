@@ -65,6 +65,7 @@ struct dfq_graph {
     // changes (the kernel's shared-memory limit is still set every launch)
     const void* cfg_kernel = nullptr;
     int cfg_smem = -1, cfg_bps = -1, cfg_grid = 0;
+    int cfg_cluster = 0;  // cluster size whose fit was checked for cfg_kernel / cfg_smem
 };
 
 namespace {
@@ -116,6 +117,9 @@ int validate_opts(const dfq_opts& o) {
     if (o.direction != 0 && o.direction != 1) return fail(DFQ_EINVAL, "direction must be 0 or 1");
     if (o.stall_test_level < 0) return fail(DFQ_EINVAL, "stall_test_level must be >= 0");
     if (o.vertex_order < 0 || o.vertex_order > 2) return fail(DFQ_EINVAL, "vertex_order must be 0, 1 or 2");
+    if (o.cluster_blocks != 0 && o.cluster_blocks != 2 && o.cluster_blocks != 4 && o.cluster_blocks != 8 &&
+        o.cluster_blocks != 16)
+        return fail(DFQ_EINVAL, "cluster_blocks must be 0, 2, 4, 8 or 16 (got %d)", o.cluster_blocks);
     const dfqk::SmemLayout L = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, true);
     const int need = L.bytes + (o.hot_cache > 0 ? 4 * dfqk::kHotWordsMax : 0);
     if (need > 227 * 1024)
@@ -417,8 +421,10 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
                int32_t* pa_host = nullptr) {
     const dfq_opts& o = g->opts;
     const bool par = parents != nullptr;
-    KernelFn k = pick_kernel(o.block_threads, par);
-    if (!k) return fail(DFQ_EINVAL, "no kernel for block_threads=%d", o.block_threads);
+    KernelFn k = o.cluster_blocks > 1 ? (KernelFn)cluster_kernel(o.block_threads, par) : pick_kernel(o.block_threads, par);
+    if (!k)
+        return fail(DFQ_EINVAL, "no kernel for block_threads=%d%s", o.block_threads,
+                    o.cluster_blocks > 1 ? " in a cluster (512 or 1024)" : "");
     const dfqk::SmemLayout lay = dfqk::smem_layout(o.block_threads, o.local_queue_cap, o.piece_edges, par);
     const int hot_words = hot_words_for(o, g->n);
     const int smem = lay.bytes + 4 * hot_words;
@@ -433,6 +439,7 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
         g->cfg_smem = smem;
         g->cfg_bps = o.blocks_per_sm;
         g->cfg_grid = g->sms * per_sm;
+        g->cfg_cluster = 0;
     }
     const int grid = g->cfg_grid;
 
@@ -470,6 +477,10 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
         return fail(DFQ_EINVAL, "direction = 1 needs a graph created with direction = 1 (checked undirected)");
     p.direction = o.direction;
     p.stall_level = o.stall_test_level;
+    // levels end on the tally barrier when its 27-bit fields hold this graph's
+    // totals exactly (fewer than 2^27 vertices and edges) and the grid's
+    // arrivals fit its 10-bit count
+    p.tally_bar = grid < 1024 ? dfqk::tally_bar_for(g->n, g->e) : 0;
     p.e = (int)g->e;
     if (g->relabeled) {
         if (par && !g->parents_int) {
@@ -491,6 +502,34 @@ int launch_bfs(dfq_graph* g, int32_t src, int32_t* levels, int32_t* parents, int
     }
 
     CUDA_TRY(cudaMemsetAsync(g->ctl, 0, sizeof(dfqk::Control), g->stream));
+    if (o.cluster_blocks > 1) {
+        // one thread-block cluster runs the BFS (its blocks are co-scheduled
+        // by the hardware, so no cooperative launch is needed)
+        const int C = o.cluster_blocks;
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)C;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3((unsigned)C);
+        cfg.blockDim = dim3((unsigned)o.block_threads);
+        cfg.dynamicSmemBytes = (size_t)smem;
+        cfg.stream = g->stream;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if (g->cfg_cluster != C) {
+            if (C > 8) CUDA_TRY(cudaFuncSetAttribute((const void*)k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+            int fits = 0;
+            CUDA_TRY(cudaOccupancyMaxActiveClusters(&fits, (const void*)k, &cfg));
+            if (fits < 1)
+                return fail(DFQ_EINVAL, "a cluster of %d blocks of %d threads with %d bytes of shared memory does not fit",
+                            C, o.block_threads, smem);
+            g->cfg_cluster = C;
+        }
+        CUDA_TRY(cudaLaunchKernelEx(&cfg, k, p));
+        return DFQ_OK;
+    }
     void* args[] = {&p};
     CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k, dim3(grid), dim3(o.block_threads), args, smem, g->stream));
     return DFQ_OK;
@@ -583,6 +622,7 @@ void dfq_opts_default(dfq_opts* o) {
     o->profile = 0;
     o->direction = 0;
     o->stall_test_level = 0;
+    o->cluster_blocks = 0;
 }
 
 int dfq_graph_create(const int32_t* offsets, const int32_t* cols, int32_t n, int64_t e, const dfq_opts* opts,

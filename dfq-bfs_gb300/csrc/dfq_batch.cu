@@ -61,14 +61,9 @@ struct BatchParams {
 };
 
 // Published-query word of a gang: release store by the gang's first block,
-// acquire loads by every member.
+// acquire loads (ld_acquire_u64) by every member.
 __device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
 }
 
 __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, int qi, const Workspace& ws) {
@@ -101,6 +96,7 @@ __device__ __forceinline__ void fill_params(Params& sp, const BatchParams& bp, i
     sp.use_tma = bp.use_tma;
     sp.timeout_ns = bp.timeout_ns;
     sp.hot_words = hot_words_of(bp.hot_words, g.n);
+    sp.tally_bar = tally_bar_for(g.n, g.e);
     remap_params(sp, g, ws);  // renumbered graphs are wide: only the grid's workspace has room
 }
 
@@ -614,6 +610,7 @@ int dfq_pool_bfs(dfq_pool* p, int32_t graph, int32_t src, int32_t* levels, int32
     prm.use_tma = o.use_tma;
     prm.timeout_ns = (long long)o.timeout_ms * 1000000LL;
     prm.hot_words = hot;
+    prm.tally_bar = grid < 1024 ? tally_bar_for(p->n[graph], p->e[graph]) : 0;
     remap_params(prm, p->h_graphs[graph], w);
     cudaEventRecord(p->ev0, p->stream);
     cudaMemsetAsync(p->d_ctl1, 0, sizeof(Control), p->stream);

@@ -67,6 +67,10 @@ struct alignas(128) LevelCtr {
     int pad1[31];
     int large_grab;                 // piece cursor over the large queue
     int pad2[31];
+    // tally barrier: the level's arrivals and tallies in two words, see
+    // tally_barrier (bits 54-63 arrivals, 27-53 and 0-26 two tallies)
+    unsigned long long tally[2];
+    int pad3[28];
 };
 
 struct DevStats {
@@ -159,7 +163,17 @@ struct Params {
     // failure-path test hook: k > 0 = at the end of level k-1 the group's last
     // block skips its barrier arrival, so every block's bounded wait runs out
     int stall_level;
+    // k > 0: multi-block groups end levels on tally_barrier with frontier
+    // edges counted in units of 2^(k-1); 0: on group_barrier
+    int tally_bar;
 };
+
+// Params::tally_bar for a graph of n vertices and e edges: the tally
+// barrier's 27-bit fields hold its level totals exactly below 2^27 of each
+// (every group has fewer than 1024 blocks, the arrival field's limit).
+__host__ __device__ inline int tally_bar_for(long long n, long long e) {
+    return (n < (1LL << 27) && e < (1LL << 27)) ? 1 : 0;
+}
 
 // Hub claim words sit a 32-byte sector apart: with hub-first ids ~1000 hubs
 // share one 128-byte bitmap line, and claim atomics on one line serialise in
@@ -193,6 +207,27 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
 }
 __device__ __forceinline__ void red_add_release(unsigned* p, unsigned v) {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_relaxed_s32(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void red_add_release_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_add_relaxed_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ void prefetch_l2(const void* p) {
     asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
@@ -347,6 +382,63 @@ __device__ __forceinline__ bool grid_barrier(Control* ctl, unsigned& target, lon
     return *s_flag != 0;
 }
 
+// Tally barrier: the grid barrier of a level's end with the level's totals
+// carried in the arrival words, so the poll that sees the last arrival also
+// returns the next level's input (the grid barrier above reads the counters
+// in one more round trip after it).  Each block adds, to two 64-bit words of
+// the level's counter slot, one arrival (bit 54) plus its tallies:
+//   w[0] = arrivals | frontier entries << 27 | frontier edges >> shift
+//   w[1] = arrivals | overflow entries << 27 | large-list pieces
+// w[1] relaxed, then w[0] with release semantics (cumulative over the
+// block's writes it observed through the block barrier).  Thread 0 polls
+// the status word and w[1] (relaxed) and w[0] (acquire), three loads in
+// flight at once, until both words hold gsize arrivals, bounded by
+// timeout_ns.  Fields are 27 bits: the host enables this barrier only for
+// graphs of fewer than 2^27 vertices and groups of fewer than 1024 blocks;
+// edges are counted in units of 2^shift (each block rounds up), so with
+// shift = 0 (graphs of fewer than 2^27 edges) the totals are exact.  The
+// slot's words are cleared with its other counters two levels ahead.
+__device__ __forceinline__ bool tally_barrier(Control* ctl, int gsize, LevelCtr* next, long long timeout_ns,
+                                              int* s_flag, int* s_in, unsigned long long w0,
+                                              unsigned long long w1, int shift, bool skip_arrive) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (!skip_arrive) {
+            red_add_relaxed_u64(&next->tally[1], w1);
+            red_add_release_u64(&next->tally[0], w0);
+        }
+        constexpr unsigned long long kMask = (1ull << 27) - 1;
+        int ok = 1;
+        unsigned long long a = 0, b = 0, t0 = 0;
+        for (unsigned it = 0;; ++it) {
+            const int st = ld_relaxed_s32(&ctl->status);
+            b = ld_relaxed_u64(&next->tally[1]);
+            a = ld_acquire_u64(&next->tally[0]);
+            if (st != 0) { ok = 0; break; }
+            if ((int)(a >> 54) == gsize && (int)(b >> 54) == gsize) break;
+            if ((it & 255) == 255) {
+                const unsigned long long now = globaltimer();
+                if (t0 == 0) t0 = now;
+                else if ((long long)(now - t0) > timeout_ns) {
+                    set_error(ctl, kErrBarrierTimeout, (int)blockIdx.x, (int)(a >> 54));
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        if (ok) {
+            s_in[0] = (int)((a >> 27) & kMask);
+            s_in[1] = (int)((b >> 27) & kMask);
+            s_in[2] = 0;
+            s_in[3] = (int)(b & kMask);
+            s_in[4] = (int)min((a & kMask) << shift, (unsigned long long)0x7fffffff);
+        }
+        *s_flag = ok;
+    }
+    __syncthreads();
+    return *s_flag != 0;
+}
+
 // Level barrier of a group of blocks running one BFS: the grid barrier above
 // for several blocks; for a one-block group, the block barrier plus thread 0
 // reading the counters its own block's atomics produced.
@@ -397,6 +489,11 @@ __host__ __device__ inline int hot_words_of(int limit_words, int n) {
     return words < limit_words ? words : limit_words;
 }
 
+// Tallies a block of a cluster group sends at the end of a level: frontier
+// entries, overflow entries, large entries, pieces, frontier edges, and 1 if
+// the block saw an error (a sum over the cluster, so every block decides alike).
+constexpr int kClTally = 6;
+
 struct SmemLayout {
     int q_off;     // local queues: 2 buffers x {start, deg, v} x cap ints
     int wl_off;    // per-warp gather scratch: {scan, start, parent} x 32 ints
@@ -446,6 +543,14 @@ struct BlockShared {
     unsigned long long large;       // entries this block sent to the large queue (whole BFS)
     unsigned long long red[2];
     int hot_off;                    // byte offset of the hot-vertex cache in dynamic shared memory
+    // cluster groups: the level barrier's mbarrier (one arrival per block of
+    // the cluster each phase), its next phase parity, the tallies this block
+    // sends at the end of a level, and three rotating slots in which every
+    // block of the cluster adds its tallies to this block's copy
+    unsigned long long cl_bar;
+    unsigned cl_parity;
+    int cl_out[kClTally];
+    int cl_in[3][kClTally];
     unsigned long long level_t0[32];  // profiling: when each warp started the level
     unsigned phase_max[4];            // profiling: this block's latest warp phase ends
 #if DFQ_CLAIM_PROBES
@@ -464,6 +569,107 @@ __device__ __forceinline__ void acc_add(int k, unsigned long long v) {
     (void)k;
     (void)v;
 #endif
+}
+
+// ------------------------------------------------------------ cluster groups
+__device__ __forceinline__ unsigned cluster_addr(const void* local, unsigned rank) {
+    unsigned a;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(local)), "r"(rank));
+    return a;
+}
+__device__ __forceinline__ void red_add_cluster(unsigned addr, int v) {
+    asm volatile("red.relaxed.cluster.shared::cluster.add.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_cluster(unsigned addr) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(addr) : "memory");
+}
+// Wait until this block's cluster mbarrier completes phase `parity` (acquire
+// at cluster scope); bounded by timeout_ns.
+__device__ __forceinline__ bool mbar_wait_cluster(unsigned long long* bar, unsigned parity, long long timeout_ns) {
+    unsigned long long t0 = 0;
+    for (unsigned it = 0;; ++it) {
+        unsigned done;
+        asm volatile(
+            "{ .reg .pred q; mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 q, [%1], %2; selp.u32 %0, 1, 0, q; }"
+            : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+        if (done) return true;
+        if ((it & 63) == 63) {
+            const unsigned long long now = globaltimer();
+            if (t0 == 0) t0 = now;
+            else if ((long long)(now - t0) > timeout_ns) return false;
+        }
+    }
+}
+// Every thread of every block of the cluster (hardware cluster barrier).  Only
+// at the start and the end of a run, which every block reaches: each wait in
+// between is bounded, and a block that gives up still comes here.
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Set up the level barrier of a cluster group of gsize blocks, then the
+// hardware barrier, so that no block reaches another's shared memory before
+// that block has initialised it.
+__device__ __forceinline__ void cluster_group_begin(int gsize) {
+    if (threadIdx.x == 0) {
+        mbar_init(&sh.cl_bar, (unsigned)gsize);
+        sh.cl_parity = 0;
+        for (int k = 0; k < kClTally; ++k) {
+            sh.cl_out[k] = 0;
+            for (int j = 0; j < 3; ++j) sh.cl_in[j][k] = 0;
+        }
+        mbar_fence_init();
+    }
+    __syncthreads();
+    cluster_sync_all();
+}
+
+// Level barrier of a cluster group.  Thread r < gsize of each block adds the
+// block's tallies (sh.cl_out) to block r's copy of slot `slot`, then arrives
+// on block r's mbarrier with release semantics at cluster scope (cumulative
+// over the block's writes it observed through the block barrier); thread 0
+// waits for its own mbarrier's phase with acquire semantics, bounded.  The
+// sums in this block's slot are then the group's, the same in every block.
+// A slot is written only at the end of a level and read after its barrier;
+// after barrier b this block clears its copy of barrier b-1's slot, which is
+// next written for barrier b+2, i.e. by blocks past barrier b+1, which needs
+// this block's arrival.  sh.cl_out is rewritten by thread 0 at the end of
+// every level, after the block barrier that ends this one.
+// first: the counters of level 0 come from the control block (set by the
+// group's first thread before the barrier).
+__device__ __forceinline__ bool cluster_barrier(Control* ctl, int gsize, int slot, long long timeout_ns,
+                                                const LevelCtr* next, bool first, bool skip_arrive) {
+    __syncthreads();
+    const int tid = (int)threadIdx.x;
+    if (tid < gsize && !skip_arrive) {
+        const unsigned base = cluster_addr(&sh.cl_in[slot][0], (unsigned)tid);
+        for (int k = 0; k < kClTally; ++k)
+            if (sh.cl_out[k]) red_add_cluster(base + 4u * k, sh.cl_out[k]);
+        mbar_arrive_cluster(cluster_addr(&sh.cl_bar, (unsigned)tid));
+    }
+    if (tid == 0) {
+        int ok = mbar_wait_cluster(&sh.cl_bar, sh.cl_parity, timeout_ns) ? 1 : 0;
+        sh.cl_parity ^= 1u;
+        if (!ok) {
+            set_error(ctl, kErrBarrierTimeout, (int)blockIdx.x, slot);
+        } else if (first) {
+            sh.in[0] = __ldcg(&next->pushed);
+            const unsigned long long op = __ldcg(&next->ovf_pieces);
+            sh.in[1] = (int)(op >> 32);
+            sh.in[2] = 0;
+            sh.in[3] = (int)(unsigned)op;
+            sh.in[4] = __ldcg(&next->pushed_edges);
+            ok = *(volatile int*)&ctl->status == 0;
+        } else {
+            for (int k = 0; k < 5; ++k) sh.in[k] = sh.cl_in[slot][k];
+            ok = sh.cl_in[slot][5] == 0;
+        }
+        const int prev = (slot + 2) % 3;  // the previous barrier's slot
+        for (int k = 0; k < kClTally; ++k) sh.cl_in[prev][k] = 0;
+        sh.flag = ok;
+    }
+    __syncthreads();
+    return sh.flag != 0;
 }
 
 // Uniform per-level values.
@@ -1100,8 +1306,9 @@ struct WarpState {
 
 // One whole BFS (init, levels, statistics) run by a group of `gsize` blocks;
 // this block is number `grank` of the group.  The group is the whole grid of
-// a cooperative launch, or a single block.  Block-collective.
-template <int B, bool PAR>
+// a cooperative launch, or a single block; with CL, the one thread-block
+// cluster of the launch (cluster barrier between levels).  Block-collective.
+template <int B, bool PAR, bool CL = false>
 __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, WarpState& ws) {
     constexpr int NW = B / 32;
     if (gsize < 1 || grank < 0 || grank >= gsize) {  // a caller bug: refuse rather than loop
@@ -1186,7 +1393,9 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
     bool bottom_up = false;
     int prev_pushed = 0;
 
-    bool ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[0], sh.in, false);
+    if constexpr (CL) cluster_group_begin(gsize);
+    bool ok = CL ? cluster_barrier(ctl, gsize, 0, p.timeout_ns, &ctl->lv[0], true, false)
+                 : group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[0], sh.in, false);
 
     for (; ok; ++L) {
         const int pushed = sh.in[0];
@@ -1205,6 +1414,8 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             cz->pushed = 0;
             cz->pushed_edges = 0;
             cz->ovf_pieces = 0ull;
+            cz->tally[0] = 0ull;
+            cz->tally[1] = 0ull;
         }
         const int in = L & 1;
         // counts past a queue's capacity (recorded as an error when pushed)
@@ -1517,6 +1728,7 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         // end of level: publish how much this block pushed, keep its queue
         __syncthreads();
         unsigned long long done_ns = 0;  // when this block finished the level (thread 0, profiling)
+        unsigned long long tw0 = 0, tw1 = 0;  // tally barrier words (thread 0)
         if (tid == 0) {
             if (p.profile) done_ns = globaltimer();
             const int kept = (int)(sh.local_pack >> 32);
@@ -1530,6 +1742,20 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
                 sh.in[2] = sh.large_pushed;
                 sh.in[3] = sh.large_pieces;
                 sh.in[4] = tot_edges;
+            } else if (CL) {
+                // a cluster group: the tallies the barrier sums over the cluster
+                sh.cl_out[0] = tot;
+                sh.cl_out[1] = sh.ovf_pushed;
+                sh.cl_out[2] = sh.large_pushed;
+                sh.cl_out[3] = sh.large_pieces;
+                sh.cl_out[4] = tot_edges;
+                sh.cl_out[5] = (s_block_err || *(volatile int*)&ctl->status != 0) ? 1 : 0;
+            } else if (p.tally_bar) {
+                constexpr unsigned long long kArrive = 1ull << 54;
+                const unsigned eu = ((unsigned)tot_edges + (1u << (p.tally_bar - 1)) - 1) >> (p.tally_bar - 1);
+                tw0 = kArrive | ((unsigned long long)(unsigned)tot << 27) | (unsigned long long)eu;
+                tw1 = kArrive | ((unsigned long long)(unsigned)sh.ovf_pushed << 27) |
+                      (unsigned long long)(unsigned)sh.large_pieces;
             } else if (tot) {
                 atomicAdd(&ctl->lv[lv.cslot].pushed, tot);
                 atomicAdd(&ctl->lv[lv.cslot].pushed_edges, tot_edges);
@@ -1544,8 +1770,13 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             sh.ovf_edges = sh.large_edges = 0;
         }
         cur ^= 1;
-        ok = group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in, true,
-                           p.stall_level == L + 1 && grank == gsize - 1);
+        const bool stall = p.stall_level == L + 1 && grank == gsize - 1;
+        ok = CL ? cluster_barrier(ctl, gsize, (L + 1) % 3, p.timeout_ns, nullptr, false, stall)
+           : (p.tally_bar && gsize > 1)
+                ? tally_barrier(ctl, gsize, &ctl->lv[(L + 1) % 3], p.timeout_ns, &sh.flag, sh.in, tw0, tw1,
+                                p.tally_bar - 1, stall)
+                : group_barrier(ctl, gsize, bar_target, p.timeout_ns, &sh.flag, &ctl->lv[(L + 1) % 3], sh.in,
+                                         true, stall);
         if (p.profile && tid == 0 && in_trace(DFQ_TSLOT(p, L))) {
             const int TL = DFQ_TSLOT(p, L);
             // recorded after the barrier: its release would otherwise wait for them
@@ -1604,6 +1835,9 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
         if (grank == 0) ctl->stats.levels = L;
     }
     __syncthreads();
+    // a cluster group's blocks leave together: none exits while another may
+    // still add to its tallies or arrive on its mbarrier
+    if constexpr (CL) cluster_sync_all();
     return ok || *(volatile int*)&ctl->status == 0;
 }
 
@@ -1626,6 +1860,16 @@ __global__ void __launch_bounds__(B, 1024 / B) dfq_bfs_kernel(const __grid_const
     init_warp_barriers<B, PAR>(p.local_cap, p.piece_edges);
     WarpState ws{0u, false};
     bfs_run<B, PAR>(p, (int)gridDim.x, (int)blockIdx.x, ws);
+}
+
+// Single-source BFS on one thread-block cluster (the launch is that cluster):
+// the cluster's hardware co-scheduling stands in for the cooperative launch,
+// and levels end on the cluster barrier in distributed shared memory.
+template <int B, bool PAR>
+__global__ void __launch_bounds__(B, 1024 / B) dfq_cluster_kernel(const __grid_constant__ Params p) {
+    init_warp_barriers<B, PAR>(p.local_cap, p.piece_edges);
+    WarpState ws{0u, false};
+    bfs_run<B, PAR, true>(p, (int)gridDim.x, (int)blockIdx.x, ws);
 }
 
 }  // namespace dfqk

@@ -141,6 +141,7 @@ __device__ __forceinline__ void serve_params(Params& sp, const ServeParams& s, c
     sp.use_tma = s.use_tma;
     sp.timeout_ns = s.timeout_ns;
     sp.hot_words = hot_words_of(s.hot_words, g.n);
+    sp.tally_bar = tally_bar_for(g.n, g.e);
     remap_params(sp, g, ws);  // renumbered graphs are wide: only the gang's workspace has room
 }
 

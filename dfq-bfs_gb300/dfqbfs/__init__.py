@@ -70,7 +70,8 @@ class Opts(C.Structure):
                 ("use_tma", C.c_int32), ("timeout_ms", C.c_int32),
                 ("wide_min_edges", C.c_int32), ("wide_min_degree", C.c_int32),
                 ("hot_cache", C.c_int32), ("vertex_order", C.c_int32), ("profile", C.c_int32),
-                ("direction", C.c_int32), ("stall_test_level", C.c_int32)]
+                ("direction", C.c_int32), ("stall_test_level", C.c_int32),
+                ("cluster_blocks", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -27,7 +27,7 @@ NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-co
                   "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
 
 HOST_SRCS = ["host_graph.cpp", "host_gen.cpp", "autotune.cpp", "host_profile.cpp"]
-CUDA_SRCS = ["dfq_api.cu", "dfq_noalloc.cu", "dfq_batch.cu", "dfq_serve.cu"]
+CUDA_SRCS = ["dfq_api.cu", "dfq_noalloc.cu", "dfq_batch.cu", "dfq_serve.cu", "dfq_cluster.cu"]
 HEADERS = ["common.hpp", "dfq_kernel.cuh", "dfq_pool.cuh"]
 
 

@@ -174,6 +174,14 @@ typedef struct dfq_opts {
                                    grid barrier, so every block's bounded wait runs out after
                                    timeout_ms and the call returns DFQ_ETIMEOUT; the graph stays
                                    usable.  Single-source launches (dfq_bfs, dfq_bfs_launch) only. */
+    int32_t cluster_blocks;     /* single-source launches: 0 (the default) = the whole GPU, one
+                                   cooperative grid with a grid barrier between levels; C in
+                                   {2, 4, 8, 16} = one thread-block cluster of C blocks runs the
+                                   BFS, its levels ending on a cluster barrier in distributed
+                                   shared memory.  For graphs whose levels stay small (grids,
+                                   meshes, road networks: thousands of levels of a few thousand
+                                   vertices); a level with millions of vertices runs on C SMs
+                                   only.  DFQ_EINVAL at launch if such a cluster does not fit. */
 } dfq_opts;
 
 typedef struct dfq_stats {

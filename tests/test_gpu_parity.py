@@ -449,7 +449,7 @@ def test_autotune_keeps_parity():
             run_and_check(g, int(s), graph=dg)
 
 
-def _check_all_sources(g, srcs, parents):
+def _check_all_sources(g, srcs, parents, opts=None):
     """Every source through dfq_bfs, bit-exact against the oracle (run on the
     host's cores in threads: ctypes releases the GIL), parents validated as a
     BFS tree, kernel E_R and reached count equal to the oracle's."""
@@ -457,7 +457,7 @@ def _check_all_sources(g, srcs, parents):
     from concurrent.futures import ThreadPoolExecutor
     oracle.lib()
     workers = min(16, os.cpu_count() or 1)
-    with d.Graph(g) as dg, ThreadPoolExecutor(max_workers=workers) as ex:
+    with d.Graph(g, opts=opts) as dg, ThreadPoolExecutor(max_workers=workers) as ex:
         wants = [ex.submit(oracle.bfs, g.offsets, g.cols, int(s)) for s in srcs]
         checks = []
         for i, s in enumerate(srcs):
