@@ -900,6 +900,48 @@ def secondary_grid(torch, d, args):
         m["host_levels"].clear()
     if not args.no_ref_gpu:
         res["reference_gpu"] = reference_gpu(g, srcs[:1], max_sources=1)
+    res["streams"] = streams_record(torch, d, args)
+    return res
+
+
+def streams_record(torch, d, args, side=1024, k=16, cluster=4, reps=3):
+    """Throughput of many high-diameter searches at once through the
+    single-graph API: k graph handles of the same side^2 grid (1 % of edges
+    deleted, largest component), each with its own stream, all k searches
+    launched (dfq_bfs_launch) before any is waited for (dfq_graph_sync).  The
+    whole-GPU cooperative kernel runs them one after another; the cluster form
+    (cluster_blocks = `cluster`, 1,024-thread blocks) runs them side by side.
+    Host wall clock from the first launch to the last sync, best of `reps`;
+    every result checked against the oracle."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+    g, _ = d.gen_grid(side, 0.01, seed=1)
+    srcs = [int(x) for x in g.pick_sources(k, seed=3)]
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        wants = list(ex.map(lambda s: oracle.bfs(g.offsets, g.cols, s), srcs))
+    res = {"graph": f"grid {side}^2, 1% edges deleted, largest component", "n": int(g.n), "searches": k}
+    for name, c in (("whole_gpu", 0), ("cluster", cluster)):
+        o = d.default_opts()
+        o.block_threads = 1024
+        o.cluster_blocks = c
+        hs = [d.Graph(g, opts=o) for _ in range(k)]
+        try:
+            lvs = [torch.empty(g.n, dtype=torch.int32, device="cuda") for _ in range(k)]
+            best = float("inf")
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for h, s, lv in zip(hs, srcs, lvs):
+                    h.launch(s, lv)
+                for h in hs:
+                    h.sync()
+                best = min(best, time.perf_counter() - t0)
+            bad = sum(oracle.compare(w, lv.cpu().numpy())["mismatches"] for w, lv in zip(wants, lvs))
+        finally:
+            for h in hs:
+                h.close()
+        res[name] = {"cluster_blocks": c, "ms_all": best * 1e3, "searches_per_s": k / best, "mismatches": int(bad)}
+    res["speedup"] = res["cluster"]["searches_per_s"] / res["whole_gpu"]["searches_per_s"]
     return res
 
 
