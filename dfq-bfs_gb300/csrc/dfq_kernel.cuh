@@ -1437,14 +1437,15 @@ __device__ __forceinline__ bool bfs_run(const Params& p, int gsize, int grank, W
             // reservation atomic and the next level's L2 read (4096^2 grid,
             // 16 sources: floors of 32, 96, 128 and 192 entries gave 7.70,
             // 7.30, 7.35 and 7.57 us a level)
+            // (32-bit divisions: every warp works these out at every level)
             const int out = max(pushed, sh.in[4] >> 3);
-            const int share = (int)(((long long)out + gsize - 1) / gsize);
-            lv.cap = min(p.local_cap, max(96, 2 * share));
+            const unsigned share = ((unsigned)out + (unsigned)gsize - 1u) / (unsigned)gsize;
+            lv.cap = (int)min((unsigned)p.local_cap, max(96u, 2u * min(share, 1u << 30)));
             // likewise in edges: while the frontier is small, the lists a block
             // finds (around hubs, long ones) go to the shared queue, where all
             // warps of the group can take them, instead of its own few warps
-            const long long eshare = ((long long)sh.in[4] + gsize - 1) / gsize;
-            lv.ecap = (int)min((long long)p.local_budget, max(1024LL, 2 * eshare));
+            const unsigned eshare = ((unsigned)sh.in[4] + (unsigned)gsize - 1u) / (unsigned)gsize;
+            lv.ecap = (int)min((unsigned)p.local_budget, max(1024u, 2u * min(eshare, 1u << 30)));
         }
         // probe-then-claim where the level scans many edges (most of them hit
         // visited vertices); claim at once, with row bounds fetched alongside,
