@@ -144,7 +144,8 @@ typedef struct dfq_opts {
                                    (multiple of 64) */
     int32_t probe_first;        /* 1: read the visited bitmap before the atomic claim;
                                    0: claim at once and fetch row bounds alongside;
-                                   2: choose per level by frontier size */
+                                   2: choose per level by frontier size (every level
+                                   probes on a graph stored hub-first) */
     int32_t l2_persist;         /* 1: visited bitmap in an L2 persisting access window */
     int32_t use_tma;            /* 1: stage large-bin pieces into smem with cp.async.bulk */
     int32_t timeout_ms;         /* bound on every device-side wait (0 = 5000) */
