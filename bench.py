@@ -512,8 +512,9 @@ def run_serve(args, torch, d):
     t_gen = time.perf_counter() - t_gen
     pool_graphs = [g for _ in range(replicas) for g in distinct]
     t_up = time.perf_counter()
-    pool = d.Pool(pool_graphs)
+    pool = d.Pool(pool_graphs, kernel_opts(d, args))
     t_up = time.perf_counter() - t_up
+    kopts = pool.opts().as_dict()
     free_b, _ = torch.cuda.mem_get_info()
     budget = int(min(48e9, free_b * 0.5))
     srv = d.Server(pool, hbm_budget_bytes=budget, ring_capacity=8192, idle_ms=20)
@@ -555,6 +556,7 @@ def run_serve(args, torch, d):
            "value": best["sustained_qps"], "unit": "queries/s", "n_gpus": 1, "steps": len(rates), "warmup": 0,
            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
            "data": "synthetic (seeded)",
+           "kernel_opts": kopts,
            "config": {"workload": "serve_poisson_40gb", "distinct_graphs": [f"{k}{a}" for k, a in specs],
                       "replicas": replicas, "pool_graphs": len(pool_graphs), "pool_gb": round(gb * replicas, 1),
                       "hbm_budget_gb": round(budget / 1e9, 1), "queries": "uniform over pool graphs, uniform "

@@ -132,7 +132,8 @@ typedef struct dfq_opts {
     int32_t block_threads;      /* threads per block: 256, 512 or 1024; 0 (the default) = by
                                    graph: 1024 when the average degree is below 8 (high-diameter
                                    graphs: fewer, larger blocks end each small level sooner),
-                                   else 512; pools and servers: 512 */
+                                   else 512; pools and servers: 1024 where the shared-memory
+                                   layout fits, else 512 */
     int32_t blocks_per_sm;      /* 0 = the occupancy limit (cooperative launch) */
     int32_t medium_min_degree;  /* deg >= this leaves the small bin (block-gathered edges)
                                    for the medium bin (one warp per vertex, int4 loads) */
