@@ -62,7 +62,8 @@ const OptField kOptFields[] = {
     {"piece_edges", &dfq_opts::piece_edges},           {"probe_first", &dfq_opts::probe_first},
     {"l2_persist", &dfq_opts::l2_persist},             {"use_tma", &dfq_opts::use_tma},
     {"timeout_ms", &dfq_opts::timeout_ms},             {"hot_cache", &dfq_opts::hot_cache},
-    {"vertex_order", &dfq_opts::vertex_order},
+    {"vertex_order", &dfq_opts::vertex_order},         {"direction", &dfq_opts::direction},
+    {"cluster_blocks", &dfq_opts::cluster_blocks},
 };
 
 // Apply "NAME=VALUE" to o; false if the name or the value is not recognised.

@@ -128,3 +128,18 @@ def test_hub_first_renumbering_on_the_host(tmp_path):
                     "-pthread"], check=True)
     r = subprocess.run([str(out)], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
+
+
+def test_opt_names(exe, tmp_path):
+    """--opt takes every kernel-shape field by name (the device double ignores
+    them) and rejects unknown names before loading anything."""
+    g = d.gen_rmat(10, 8, seed=53)
+    g.source = int(g.pick_sources(1, seed=53)[0])
+    g.save(tmp_path / "g.dat", "dat")
+    args = [str(exe), str(tmp_path / "g.dat")]
+    for kv in ("cluster_blocks=8", "direction=0", "probe_first=1", "block_threads=1024"):
+        r = subprocess.run(args + ["--opt", kv], capture_output=True, text=True)
+        assert r.returncode == 0, (kv, r.stderr)
+        assert field(r.stdout, r"- Error = (\d+)") == ["0"]
+    r = subprocess.run(args + ["--opt", "no_such_field=1"], capture_output=True, text=True)
+    assert r.returncode == 2 and "dfq_opts field" in r.stderr
