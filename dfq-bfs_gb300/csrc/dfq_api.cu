@@ -384,7 +384,7 @@ int maybe_relabel(dfq_graph* g) {
     g->rank_host = std::move(rank);
     g->relabeled = true;
     // hubs (now the smallest ids) get claim words of their own
-    g->hub_n = std::min<int32_t>(n, dfqk::kHubIds);
+    g->hub_n = dfqk::hub_count(n);
     if ((rc = dev_alloc(&g->hub_claim, (size_t)g->hub_n * dfqk::kHubStride))) return rc;
     return DFQ_OK;
 }

@@ -84,7 +84,7 @@ __host__ __device__ inline void remap_params(Params& sp, const PoolGraph& g, con
     sp.order = g.order;
     sp.map_src = 1;
     sp.hub_claim = ws.hub_claim;
-    sp.hub_n = g.n < kHubIds ? g.n : kHubIds;
+    sp.hub_n = hub_count(g.n);
 }
 
 }  // namespace dfqk
