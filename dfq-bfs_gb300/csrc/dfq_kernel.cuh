@@ -917,12 +917,16 @@ __device__ __forceinline__ void claim4(const Params& p, const Lv& lv, Tally& t, 
 #endif
     };
     probe_at(0, (unsigned)v[0]);
+    // claim-at-once levels load the row bounds alongside the claim atomics;
+    // probe levels, whose candidates often lose the claim (many warps met
+    // the same vertex), load them for the winners only (RMAT-22 0.4747 ->
+    // 0.4718 ms)
     int so[4], eo[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         so[j] = 0;
         eo[j] = 0;
-        if (vm >> j & 1) {
+        if (!lv.probe && (vm >> j & 1)) {
             so[j] = __ldg(p.offsets + v[j]);
             eo[j] = __ldg(p.offsets + v[j] + 1);
         }
@@ -951,6 +955,14 @@ __device__ __forceinline__ void claim4(const Params& p, const Lv& lv, Tally& t, 
             if (v[j] < p.hub_n) atomicOr(&p.bitmap[v[j] >> 5], bit);
         }
         hot_learn(lv, v[j]);  // visited now, whoever won
+    }
+    if (lv.probe) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (won >> j & 1) {
+                so[j] = __ldg(p.offsets + v[j]);
+                eo[j] = __ldg(p.offsets + v[j] + 1);
+            }
     }
     int st[4], dg[4];
     unsigned loc = 0, lm = 0;
