@@ -42,6 +42,7 @@ def test_option_struct_layout_matches_header():
     assert all(t is C.c_int32 for _, t in d.Opts._fields_)
     o = d.default_opts()
     assert o.stall_test_level == 0 and o.direction == 0 and o.timeout_ms == 5000
+    assert o.cluster_blocks == 0 and o.probe_first == 2 and o.block_threads == 0
 
 
 def test_struct_mirrors_match_the_c_layout(tmp_path):
